@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 batched C2C FFT (one JSON line on rank 0).
+
+Headline workload (default): N = 4096, batch = 16384 (2^26 samples, 512 MB
+complex64), re/im iid N(0,1) from the seeded PCG generator (seed 2).  One
+step = one forward transform of the whole batch followed by one inverse
+transform of its spectrum (out of place, x -> X -> x'), i.e. 2 * N * batch
+samples transformed per step.  Inputs are resident in HBM before the timed
+region; 512 MB per operand is larger than L2 (129 MB), so no L2 flush is
+needed between steps.
+
+  value      GSamples/s over the timed steps (CUDA events on the launching
+             stream, max over ranks), samples counted per transform
+  e2e        same metric through the host C-ABI entry gbfft_c2c_host from
+             pinned host memory (H2D + transform + D2H inside the timed region)
+  roofline   achieved HBM GB/s of the dominant kernel (16 bytes per sample
+             per launch: one complex64 read + one write) vs the measured copy
+             bandwidth
+  cpu_baseline  the reference's Stockham R4/R2 path restated in C (the
+             oracle), all host threads, on a bounded sample of the workload
+
+--impl reference times that CPU restatement alone on the same config.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "wgls-rs-fft_gb300"))
+
+WORKLOADS = {
+    # name: (log2 N, batch, distribution, seed)
+    "n4096_b16384": (12, 16384, "normal", 2),
+    "n1024_b9": (10, 9, "uniform", 1),
+    "n256_b262144": (8, 262144, "normal", 2),
+    "n512_b131072": (9, 131072, "normal", 2),
+    "n1024_b65536": (10, 65536, "normal", 2),
+    "n2048_b32768": (11, 32768, "normal", 2),
+    "n8192_b8192": (13, 8192, "normal", 2),
+    "n16384_b4096": (14, 4096, "normal", 2),
+    "n65536_b4096": (16, 4096, "normal", 2),
+    "n4194304_b64": (22, 64, "normal", 3),
+    "n16777216_b4": (24, 4, "normal", 3),
+    "n67108864_b1": (26, 1, "normal", 3),
+}
+DEFAULT_WORKLOAD = "n4096_b16384"
+METRIC = "batched C2C FFT GSamples/s + % HBM roofline; TC-split vs FP32 @ relL2<=2e-6"
+UNIT = "GSamples/s"
+
+
+def rank_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def passes_for(logn: int) -> int:
+    if logn <= 14:
+        return 1
+    return max(2, (logn + 9) // 10)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(workload: str):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (line 'traffic_bytes_per_launch: <int>'), else None."""
+    path = os.path.join(ROOT, "profiles", f"fft_{workload}.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1].strip()))
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the GPU works."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.time(), line.strip()))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for _, line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_input(logn, batch, dist, seed, device):
+    from gbfft import signals
+    if dist == "normal":
+        return signals.normal_c64_torch(batch, 1 << logn, seed, device=device)
+    return signals.uniform_c64_torch(batch, 1 << logn, seed, device=device)
+
+
+def cpu_reference_rate(logn, batch, rows, seconds_budget, threads):
+    """The reference path restated in C (oracle), all threads, over `rows`
+    rows of the workload, forward + inverse; returns (GSamples/s, rows, reps)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from gbfft import signals
+    oracle.build()
+    n = 1 << logn
+    rows = max(1, min(rows, batch))
+    x = signals.normal_c64(rows, n, seed=2)
+    oracle.ref_fft(x, False, threads)  # warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        y = oracle.ref_fft(x, False, threads)
+        oracle.ref_fft(y, True, threads)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds_budget:
+            break
+    return 2.0 * rows * n * reps / el / 1e9, rows, reps
+
+
+def run_reference_arm(args, workload):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return 0
+    logn, batch, dist, seed = WORKLOADS[workload]
+    n = 1 << logn
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from gbfft import signals
+    oracle.build()
+    threads = os.cpu_count() or 1
+    rows = max(threads, min(batch, 256 if n <= 4096 else max(1, (1 << 20) // n)))
+    x = signals.normal_c64(rows, n, seed=seed) if dist == "normal" else signals.uniform_c64(rows, n, seed=seed)
+    for _ in range(args.warmup):
+        oracle.ref_fft(oracle.ref_fft(x, False, threads), True, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.ref_fft(oracle.ref_fft(x, False, threads), True, threads)
+    el = time.perf_counter() - t0
+    value = 2.0 * rows * n * args.steps / el / 1e9
+    sample = (f"{rows} of {batch} rows of N={n} per step (forward + inverse), "
+              f"reference Stockham R4/R2 f32 path restated in C, {threads} threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded PCG, N(0,1))",
+        "config": {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse",
+                   "l2": "n/a (host)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    workload = args.workload
+
+    if args.impl == "reference":
+        return run_reference_arm(args, workload)
+
+    import torch
+    import gbfft
+
+    rank, world, local = rank_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    gbfft.build()
+    ctx = gbfft.Context(local)
+
+    logn, batch, distn, seed = WORKLOADS[workload]
+    n = 1 << logn
+    x = make_input(logn, batch, distn, seed, dev)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step():
+        ctx.c2c_device(x, y, n, batch, gbfft.FORWARD, stream=sp)
+        ctx.c2c_device(y, z, n, batch, gbfft.INVERSE, stream=sp)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = ctx.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    sampler.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = ctx.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    samples_per_step = 2 * n * batch
+    value = samples_per_step * args.steps * world / (ms * 1e-3) / 1e9
+
+    # roofline of the dominant kernel (every launch reads and writes each sample once)
+    launch_s = ms * 1e-3 / max(1, launches)
+    alg_bytes = 16 * n * batch
+    achieved = alg_bytes / launch_s / 1e9
+    peak, peak_kind = peaks()
+    traffic = profile_traffic(workload)
+
+    # check the last step's roundtrip (cheap, catches a broken build)
+    rt = (torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x)).item()
+
+    # end to end through the host C ABI from pinned memory
+    e2e = None
+    if not args.no_e2e:
+        hx = x.cpu().pin_memory()
+        hy = torch.empty_like(hx).pin_memory()
+        hz = torch.empty_like(hx).pin_memory()
+        ctx.c2c_host_ptr(hx.data_ptr(), hy.data_ptr(), n, batch, gbfft.FORWARD)  # warm
+        ctx.c2c_host_ptr(hy.data_ptr(), hz.data_ptr(), n, batch, gbfft.INVERSE)
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            ctx.c2c_host_ptr(hx.data_ptr(), hy.data_ptr(), n, batch, gbfft.FORWARD)
+            ctx.c2c_host_ptr(hy.data_ptr(), hz.data_ptr(), n, batch, gbfft.INVERSE)
+        el = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([el], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            el = float(t.item())
+        nbytes = 8 * n * batch
+        e2e = {"value": samples_per_step * args.e2e_steps * world / el / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
+               "steps": args.e2e_steps, "api": "gbfft_c2c_host (pinned host buffers)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rows = 256 if n <= 4096 else max(1, (1 << 20) // n)
+        v, rows, reps = cpu_reference_rate(logn, batch, rows, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{rows} of {batch} rows of N={n}, forward+inverse, repeated {reps}x "
+                         f"(~{args.cpu_seconds:.0f} s); reference Stockham R4/R2 f32 path restated in C"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded PCG hash, re/im iid " + ("N(0,1))" if distn == "normal" else "U[-1,1))"),
+            "config": {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse",
+                       "placement": "out-of-place", "form": "fp32 single-pass" if logn <= 14 else
+                       f"fp32 {passes_for(logn)}-pass", "l2": "inputs (512 MB) larger than L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "alg_bytes_per_launch": alg_bytes, "launch_us": launch_s * 1e6},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": sampler.summary(),
+            "roundtrip_rel_l2": rt,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

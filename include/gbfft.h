@@ -1,0 +1,122 @@
+/*
+ * gbfft -- batched power-of-two complex-to-complex FFT for GB300 (sm_103a).
+ *
+ * C ABI behind which the GB300 kernels sit.  It is the boundary a binding of
+ * larsjoost/wgls-rs-fft's `GpuFft` (src/lib.rs:75-950) calls: plain pointers
+ * and sizes, no CUDA or torch types in the signatures (streams are `void*`
+ * holding a cudaStream_t).
+ *
+ * Data layout: complex<f32> interleaved (re, im), transforms stored
+ * back-to-back (batch-major), exactly the layout the reference uploads
+ * (src/lib.rs:539-548).
+ *
+ * Transform definitions (src/lib.rs:433-488):
+ *   forward  (GBFFT_FORWARD):  X_k = sum_n x_n e^{-2 pi i k n / N}   (unscaled)
+ *   inverse  (GBFFT_INVERSE):  x_n = (1/N) sum_k X_k e^{+2 pi i k n / N}
+ * The reference computes the inverse as conj(FFT(conj x)) * (1/N)
+ * (src/lib.rs:571-579, 661-669); that is the same transform.
+ *
+ * A context is not thread-safe: use one per host thread, as the reference's
+ * GpuFft (RefCell cache, src/lib.rs:81) is single-threaded.
+ */
+#ifndef GBFFT_H
+#define GBFFT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBFFT_FORWARD (-1)
+#define GBFFT_INVERSE (+1)
+
+/* Status codes.  Messages for the first two are the reference's own strings. */
+typedef enum gbfft_status {
+    GBFFT_OK = 0,
+    /* "Transform length must be a non-zero power of two" (src/lib.rs:506-511) */
+    GBFFT_ERR_INVALID_SIZE = 1,
+    /* "All input vectors in a batch must have the same length" (src/lib.rs:526-533) */
+    GBFFT_ERR_LENGTH_MISMATCH = 2,
+    GBFFT_ERR_INVALID_ARGUMENT = 3, /* null pointer, bad direction or precision */
+    GBFFT_ERR_NO_DEVICE = 4,        /* no usable GB300 (sm_103) device */
+    GBFFT_ERR_OUT_OF_MEMORY = 5,    /* device or pinned host allocation failed */
+    GBFFT_ERR_CUDA = 6,             /* a CUDA runtime call failed; see gbfft_last_error */
+    GBFFT_ERR_TIMEOUT = 7,          /* a bounded device-side wait gave up */
+    GBFFT_ERR_UNSUPPORTED = 8       /* size/precision combination not provided */
+} gbfft_status;
+
+/* Arithmetic used for the butterflies. */
+typedef enum gbfft_precision {
+    GBFFT_PREC_FP32 = 0 /* plain FP32 Stockham form */
+} gbfft_precision;
+
+typedef struct gbfft_ctx gbfft_ctx;
+
+/* Replaces GpuFft::is_gpu_available (src/lib.rs:381-389): 1 when a usable
+ * sm_103 device is present, else 0.  Creates no context. */
+int gbfft_is_available(void);
+
+/* Replaces GpuFft::new (src/lib.rs:285-330): selects `device`, creates the
+ * context's stream.  No kernel JIT; plans are built on first use of a size. */
+int gbfft_create(int device, gbfft_ctx **out_ctx);
+
+/* Replaces Drop for GpuFft: frees plans, device buffers, pinned staging. */
+void gbfft_destroy(gbfft_ctx *ctx);
+
+/* Message for the most recent failing call on `ctx` ("" if none).  The string
+ * is owned by the context and valid until the next call on it. */
+const char *gbfft_last_error(const gbfft_ctx *ctx);
+
+/* Static description of a status code. */
+const char *gbfft_status_string(int status);
+
+/* Replaces GpuFft::fft / GpuFft::ifft (src/lib.rs:433-438, 483-488) via
+ * transform_batch_internal (src/lib.rs:517-568) for a contiguous host batch:
+ * `in` and `out` hold batch*n interleaved complex<f32> (they may alias).
+ * Copies to the device, transforms, copies back and returns when `out` holds
+ * the result.  batch == 0 returns GBFFT_OK without touching the pointers
+ * (src/lib.rs:522-524). */
+int gbfft_c2c_host(gbfft_ctx *ctx, const float *in, float *out, uint64_t n,
+                   uint64_t batch, int direction);
+
+/* Same, for the reference's own argument shape &[Vec<Complex<f32>>]
+ * (src/lib.rs:433, 517-533): `batch` separate rows, row i at in_rows[i] with
+ * row_lengths[i] complex values, result row i written to out_rows[i].
+ * All lengths must be equal (GBFFT_ERR_LENGTH_MISMATCH) and a power of two
+ * (GBFFT_ERR_INVALID_SIZE), checked in the reference's order. */
+int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows,
+                        const uint64_t *row_lengths, float *const *out_rows,
+                        uint64_t batch, int direction);
+
+/* Device-resident entry point (new; no reference counterpart -- the reference
+ * always round-trips through host memory).  `d_in`/`d_out` are device
+ * pointers to batch*n interleaved complex<f32>; they may alias.  Work is
+ * enqueued on `stream` (a cudaStream_t; NULL selects the context's stream)
+ * and the call returns without synchronising. */
+int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,
+                     uint64_t batch, int direction, void *stream);
+
+/* Replaces GpuFftTrait::benchmark_gpu_only (src/lib.rs:108-156, 673-707):
+ * device-only timing of `iters` transforms of an n x batch device batch after
+ * `warmup` untimed ones, with CUDA events on the context's stream.  Writes the
+ * mean seconds per transform. */
+int gbfft_bench_device(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction,
+                       int warmup, int iters, double *seconds_per_iter);
+
+/* Select the butterfly arithmetic for later calls on `ctx`. */
+int gbfft_set_precision(gbfft_ctx *ctx, int precision);
+
+/* Number of kernel launches this context has issued since creation (all
+ * entry points).  Lets callers count GPU work without a profiler. */
+uint64_t gbfft_launch_count(const gbfft_ctx *ctx);
+
+/* Library version string. */
+const char *gbfft_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFFT_H */

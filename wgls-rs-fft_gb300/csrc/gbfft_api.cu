@@ -1,0 +1,353 @@
+// C ABI of the GB300 FFT (declared in include/gbfft.h).
+//
+// Mirrors the reference's GpuFft (larsjoost/wgls-rs-fft src/lib.rs:75-950):
+//   GpuFft::new                  -> gbfft_create        (src/lib.rs:285-330)
+//   GpuFft::is_gpu_available     -> gbfft_is_available  (src/lib.rs:381-389)
+//   GpuFft::fft / ifft           -> gbfft_c2c_host(_rows) (src/lib.rs:433-568)
+//   SizeCache / build_size_cache -> Plan / plan_for     (src/lib.rs:230-259, 709-943)
+//   benchmark_gpu_only           -> gbfft_bench_device  (src/lib.rs:673-707)
+// plus the device-resident entry gbfft_c2c_device.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gbfft_internal.h"
+#include "gbfft_plan.h"
+
+using namespace gbfft;
+
+struct gbfft_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t xfer[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::string err;
+    std::map<int, std::unique_ptr<Plan>> plans;
+    DeviceBuffer dbuf;    // device copy of a host batch
+    DeviceBuffer ws;      // multi-pass workspace
+    void *hstage = nullptr;
+    size_t hstage_bytes = 0;
+    uint64_t launches = 0;
+    int precision = GBFFT_PREC_FP32;
+};
+
+namespace {
+
+const char *kMsgInvalidSize = "Transform length must be a non-zero power of two";
+const char *kMsgLengthMismatch = "All input vectors in a batch must have the same length";
+
+int fail(gbfft_ctx *ctx, int status, const char *fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return status;
+}
+
+int cuda_fail(gbfft_ctx *ctx, cudaError_t e, const char *what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ctx, GBFFT_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(ctx, GBFFT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define GB_CUDA(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+bool is_pow2(uint64_t n) { return n != 0 && (n & (n - 1)) == 0; }
+int log2u(uint64_t n) {
+    int l = 0;
+    while ((1ull << l) < n) ++l;
+    return l;
+}
+
+bool device_supported(int dev) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, dev) != cudaSuccess) return false;
+    return p.major == 10 && p.minor == 3;  // kernels are built for sm_103a only
+}
+
+int host_is_pinned(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+int ensure_hstage(gbfft_ctx *ctx, size_t bytes) {
+    if (ctx->hstage_bytes >= bytes) return GBFFT_OK;
+    if (ctx->hstage) cudaFreeHost(ctx->hstage);
+    ctx->hstage = nullptr;
+    ctx->hstage_bytes = 0;
+    cudaError_t e = cudaHostAlloc(&ctx->hstage, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, GBFFT_ERR_OUT_OF_MEMORY, "pinned staging of %zu bytes: %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    ctx->hstage_bytes = bytes;
+    return GBFFT_OK;
+}
+
+int get_plan(gbfft_ctx *ctx, int logn, Plan **out) {
+    auto it = ctx->plans.find(logn);
+    if (it != ctx->plans.end()) {
+        *out = it->second.get();
+        return GBFFT_OK;
+    }
+    std::unique_ptr<Plan> p(new Plan());
+    std::string why;
+    int st = plan_build(*p, logn, ctx->stream, why);
+    if (st != GBFFT_OK) return fail(ctx, st, "plan for N=2^%d: %s", logn, why.c_str());
+    *out = p.get();
+    ctx->plans[logn] = std::move(p);
+    return GBFFT_OK;
+}
+
+int validate_common(gbfft_ctx *ctx, uint64_t n, int direction) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (direction != GBFFT_FORWARD && direction != GBFFT_INVERSE)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "direction must be -1 (forward) or +1 (inverse)");
+    if (!is_pow2(n)) return fail(ctx, GBFFT_ERR_INVALID_SIZE, "%s", kMsgInvalidSize);
+    if (log2u(n) > kMaxLogN)
+        return fail(ctx, GBFFT_ERR_UNSUPPORTED, "transform length 2^%d exceeds 2^%d", log2u(n), kMaxLogN);
+    return GBFFT_OK;
+}
+
+// Enqueue one transform of the whole device batch on `stream`.
+int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
+               cudaStream_t stream) {
+    Plan *plan = nullptr;
+    int st = get_plan(ctx, log2u(n), &plan);
+    if (st != GBFFT_OK) return st;
+    uint64_t launches = 0;
+    std::string why;
+    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, stream, launches, why);
+    ctx->launches += launches;
+    if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
+                                    (unsigned long long)batch, why.c_str());
+    return GBFFT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gbfft_version(void) { return "gbfft 0.1 (sm_103a)"; }
+
+const char *gbfft_status_string(int s) {
+    switch (s) {
+        case GBFFT_OK: return "ok";
+        case GBFFT_ERR_INVALID_SIZE: return kMsgInvalidSize;
+        case GBFFT_ERR_LENGTH_MISMATCH: return kMsgLengthMismatch;
+        case GBFFT_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case GBFFT_ERR_NO_DEVICE: return "no usable sm_103 GPU";
+        case GBFFT_ERR_OUT_OF_MEMORY: return "out of memory";
+        case GBFFT_ERR_CUDA: return "CUDA error";
+        case GBFFT_ERR_TIMEOUT: return "device-side wait timed out";
+        case GBFFT_ERR_UNSUPPORTED: return "unsupported size or precision";
+        default: return "unknown status";
+    }
+}
+
+int gbfft_is_available(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    for (int d = 0; d < n; ++d)
+        if (device_supported(d)) return 1;
+    return 0;
+}
+
+int gbfft_create(int device, gbfft_ctx **out_ctx) {
+    if (!out_ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    *out_ctx = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return GBFFT_ERR_NO_DEVICE;
+    }
+    if (!device_supported(device)) return GBFFT_ERR_NO_DEVICE;
+    if (cudaSetDevice(device) != cudaSuccess) return GBFFT_ERR_CUDA;
+    std::unique_ptr<gbfft_ctx> ctx(new gbfft_ctx());
+    ctx->device = device;
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return GBFFT_ERR_CUDA;
+    for (auto &s : ctx->xfer)
+        if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return GBFFT_ERR_CUDA;
+    if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
+        return GBFFT_ERR_CUDA;
+    *out_ctx = ctx.release();
+    return GBFFT_OK;
+}
+
+void gbfft_destroy(gbfft_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &s : ctx->xfer)
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    ctx->plans.clear();
+    ctx->dbuf.release();
+    ctx->ws.release();
+    if (ctx->hstage) cudaFreeHost(ctx->hstage);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *gbfft_last_error(const gbfft_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+uint64_t gbfft_launch_count(const gbfft_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int gbfft_set_precision(gbfft_ctx *ctx, int precision) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (precision != GBFFT_PREC_FP32)
+        return fail(ctx, GBFFT_ERR_UNSUPPORTED, "precision %d is not provided", precision);
+    ctx->precision = precision;
+    return GBFFT_OK;
+}
+
+int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n, uint64_t batch, int direction,
+                     void *stream) {
+    int st = validate_common(ctx, n, direction);
+    if (st != GBFFT_OK) return st;
+    if (batch == 0) return GBFFT_OK;
+    if (!d_in || !d_out) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null device pointer");
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    return run_device(ctx, (const float2 *)d_in, (float2 *)d_out, n, batch, direction, s);
+}
+
+// Host batch already contiguous in `in` (pinned or pageable).
+static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t n, uint64_t batch,
+                           int direction) {
+    const size_t bytes = (size_t)n * batch * sizeof(float2);
+    int st = ctx->dbuf.ensure(bytes, ctx->err);
+    if (st != GBFFT_OK) return st;
+    float2 *d = (float2 *)ctx->dbuf.ptr;
+    const bool pinned = host_is_pinned(in) && host_is_pinned(out);
+    const float *src = in;
+    float *dst = out;
+    if (!pinned) {
+        st = ensure_hstage(ctx, bytes);
+        if (st != GBFFT_OK) return st;
+        memcpy(ctx->hstage, in, bytes);
+        src = (const float *)ctx->hstage;
+        dst = (float *)ctx->hstage;
+    }
+    // Split the batch into chunks of whole transforms and pipeline
+    // H2D -> transform -> D2H over three streams so the two copy directions and
+    // the kernels overlap.
+    Plan *plan = nullptr;
+    st = get_plan(ctx, log2u(n), &plan);
+    if (st != GBFFT_OK) return st;
+    const size_t row_bytes = (size_t)n * sizeof(float2);
+    const size_t chunk_target = (size_t)32 << 20;
+    uint64_t rows_per_chunk = row_bytes >= chunk_target ? 1 : chunk_target / row_bytes;
+    if (plan->needs_workspace) rows_per_chunk = batch;  // one workspace: no overlap
+    uint64_t done = 0;
+    int k = 0;
+    while (done < batch) {
+        const uint64_t rows = (batch - done) < rows_per_chunk ? (batch - done) : rows_per_chunk;
+        const size_t off = (size_t)done * row_bytes;
+        const size_t len = (size_t)rows * row_bytes;
+        cudaStream_t s = ctx->xfer[k % 3];
+        GB_CUDA(ctx, cudaMemcpyAsync((char *)d + off, (const char *)src + off, len, cudaMemcpyHostToDevice, s));
+        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)d + off), n, rows, direction, s);
+        if (st != GBFFT_OK) return st;
+        GB_CUDA(ctx, cudaMemcpyAsync((char *)dst + off, (char *)d + off, len, cudaMemcpyDeviceToHost, s));
+        done += rows;
+        ++k;
+    }
+    for (auto s : ctx->xfer) GB_CUDA(ctx, cudaStreamSynchronize(s));
+    if (!pinned) memcpy(out, ctx->hstage, bytes);
+    return GBFFT_OK;
+}
+
+int gbfft_c2c_host(gbfft_ctx *ctx, const float *in, float *out, uint64_t n, uint64_t batch, int direction) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (batch == 0) return GBFFT_OK;  // src/lib.rs:522-524
+    int st = validate_common(ctx, n, direction);
+    if (st != GBFFT_OK) return st;
+    if (!in || !out) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null host pointer");
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    return host_contiguous(ctx, in, out, n, batch, direction);
+}
+
+int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows, const uint64_t *row_lengths,
+                        float *const *out_rows, uint64_t batch, int direction) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (batch == 0) return GBFFT_OK;  // src/lib.rs:522-524
+    if (!in_rows || !row_lengths || !out_rows)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null row array");
+    // src/lib.rs:526-533: equal lengths, then power of two, row by row.
+    const uint64_t n = row_lengths[0];
+    for (uint64_t i = 0; i < batch; ++i) {
+        if (row_lengths[i] != n) return fail(ctx, GBFFT_ERR_LENGTH_MISMATCH, "%s", kMsgLengthMismatch);
+        if (!is_pow2(row_lengths[i])) return fail(ctx, GBFFT_ERR_INVALID_SIZE, "%s", kMsgInvalidSize);
+    }
+    int st = validate_common(ctx, n, direction);
+    if (st != GBFFT_OK) return st;
+    for (uint64_t i = 0; i < batch; ++i)
+        if (!in_rows[i] || !out_rows[i]) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null row pointer");
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t row_bytes = (size_t)n * sizeof(float2);
+    const size_t bytes = row_bytes * batch;
+    st = ensure_hstage(ctx, bytes);
+    if (st != GBFFT_OK) return st;
+    char *stage = (char *)ctx->hstage;
+    for (uint64_t i = 0; i < batch; ++i) memcpy(stage + i * row_bytes, in_rows[i], row_bytes);
+    st = host_contiguous(ctx, (const float *)stage, (float *)stage, n, batch, direction);
+    if (st != GBFFT_OK) return st;
+    for (uint64_t i = 0; i < batch; ++i) memcpy(out_rows[i], stage + i * row_bytes, row_bytes);
+    return GBFFT_OK;
+}
+
+int gbfft_bench_device(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, int warmup, int iters,
+                       double *seconds_per_iter) {
+    int st = validate_common(ctx, n, direction);
+    if (st != GBFFT_OK) return st;
+    if (!seconds_per_iter || iters <= 0 || warmup < 0 || batch == 0)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "bad benchmark arguments");
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = (size_t)n * batch * sizeof(float2);
+    st = ctx->dbuf.ensure(bytes, ctx->err);
+    if (st != GBFFT_OK) return st;
+    float2 *d = (float2 *)ctx->dbuf.ptr;
+    GB_CUDA(ctx, cudaMemsetAsync(d, 0, bytes, ctx->stream));
+    for (int i = 0; i < warmup; ++i) {
+        st = run_device(ctx, d, d, n, batch, direction, ctx->stream);
+        if (st != GBFFT_OK) return st;
+    }
+    GB_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+    for (int i = 0; i < iters; ++i) {
+        st = run_device(ctx, d, d, n, batch, direction, ctx->stream);
+        if (st != GBFFT_OK) return st;
+    }
+    GB_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+    GB_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    float ms = 0.f;
+    GB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    *seconds_per_iter = (double)ms * 1e-3 / iters;
+    return GBFFT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,188 @@
+// Plan construction and execution (see gbfft_plan.h).
+#include <algorithm>
+#include <cstring>
+
+#include "gbfft_plan.h"
+
+namespace gbfft {
+
+int DeviceBuffer::ensure(size_t want, std::string &err) {
+    if (bytes >= want) return GBFFT_OK;
+    release();
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        ptr = nullptr;
+        err = std::string("device allocation of ") + std::to_string(want) + " bytes: " + cudaGetErrorString(e);
+        return GBFFT_ERR_OUT_OF_MEMORY;
+    }
+    bytes = want;
+    return GBFFT_OK;
+}
+
+void DeviceBuffer::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+Plan::~Plan() {
+    if (tw) cudaFree(tw);
+}
+
+// Split log2 N into global-pass radices 2^5..2^10, largest first.
+std::vector<int> split_passes(int logn) {
+    int p = (logn + 9) / 10;
+    if (p < 2) p = 2;
+    std::vector<int> parts(p, logn / p);
+    for (int i = 0; i < logn % p; ++i) parts[i] += 1;
+    return parts;
+}
+
+static void add_sub_segments(std::vector<TwiddleSegment> &segs, uint64_t base, const std::vector<int> &logr,
+                             const std::vector<int> &logp) {
+    uint64_t off = base;
+    for (size_t i = 1; i < logr.size(); ++i) {
+        TwiddleSegment s;
+        s.offset = off;
+        s.count = (uint64_t)((1 << logr[i]) - 1) << logp[i];
+        s.kind = 0;
+        s.logm = logr[i] + logp[i];
+        s.logp = logp[i];
+        s.logstride = 0;
+        segs.push_back(s);
+        off += s.count;
+    }
+}
+
+static uint64_t sub_entries(const std::vector<int> &logr, const std::vector<int> &logp) {
+    uint64_t n = 0;
+    for (size_t i = 1; i < logr.size(); ++i) n += (uint64_t)((1 << logr[i]) - 1) << logp[i];
+    return n;
+}
+
+int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
+    p.logn = logn;
+    std::vector<TwiddleSegment> segs;
+    cudaError_t e;
+    if (logn <= kRowsMaxLogN) {
+        if (!rows_kernel_info(logn, p.rows)) {
+            why = "no single-pass kernel";
+            return GBFFT_ERR_UNSUPPORTED;
+        }
+        if ((e = rows_prepare(p.rows)) != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        std::vector<int> lr(p.rows.sub_logr, p.rows.sub_logr + p.rows.nsub);
+        std::vector<int> lp(p.rows.sub_logp, p.rows.sub_logp + p.rows.nsub);
+        add_sub_segments(segs, 0, lr, lp);
+        p.tw_entries = p.rows.tw_entries;
+    } else {
+        p.multipass = true;
+        p.needs_workspace = true;
+        std::vector<int> parts = split_passes(logn);
+        uint64_t off = 0;
+        int logp = 0;
+        for (size_t i = 0; i < parts.size(); ++i) {
+            PassDesc d;
+            std::vector<int> lr, lp;
+            if (!pass_kernel_info(parts[i], i == 0, d, lr, lp)) {
+                why = "no pass kernel for radix 2^" + std::to_string(parts[i]);
+                return GBFFT_ERR_UNSUPPORTED;
+            }
+            if ((e = pass_prepare(d)) != cudaSuccess) {
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_CUDA;
+            }
+            d.logp = logp;
+            d.sub_tw_offset = off;
+            add_sub_segments(segs, off, lr, lp);
+            off += sub_entries(lr, lp);
+            logp += parts[i];
+            p.passes.push_back(d);
+        }
+        p.tw_split = (logn + 1) / 2;
+        p.tw_lo_offset = off;
+        TwiddleSegment lo = {off, 1ull << p.tw_split, 1, logn, 0, 0};
+        off += lo.count;
+        p.tw_hi_offset = off;
+        TwiddleSegment hi = {off, 1ull << (logn - p.tw_split), 1, logn, 0, p.tw_split};
+        off += hi.count;
+        segs.push_back(lo);
+        segs.push_back(hi);
+        p.tw_entries = off;
+    }
+    if (p.tw_entries > 0) {
+        if ((e = cudaMalloc(&p.tw, p.tw_entries * sizeof(float2))) != cudaSuccess) {
+            cudaGetLastError();
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_OUT_OF_MEMORY;
+        }
+        if ((e = twiddle_fill(p.tw, segs.data(), (int)segs.size(), stream)) != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+    }
+    return GBFFT_OK;
+}
+
+int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction, DeviceBuffer &ws,
+                 cudaStream_t stream, uint64_t &launches, std::string &why) {
+    launches = 0;
+    if (batch == 0) return GBFFT_OK;
+    cudaError_t e;
+    if (!p.multipass) {
+        e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, stream);
+        if (e != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        launches = 1;
+        return GBFFT_OK;
+    }
+    const int np = (int)p.passes.size();
+    const size_t bytes = ((size_t)batch << p.logn) * sizeof(float2);
+    // Buffer routing.  Pass np-1 may run in place (each CTA reads and writes
+    // the same samples); earlier passes must not.  Option A ends pass np-2 in
+    // `out`, option B in the workspace.
+    std::vector<const float2 *> src(np);
+    std::vector<float2 *> dst(np);
+    auto route = [&](bool last_in_place, float2 *w) {
+        for (int i = 0; i < np - 1; ++i) {
+            const bool to_out = ((np - 2 - i) % 2 == 0) == last_in_place;
+            dst[i] = to_out ? out : w;
+        }
+        dst[np - 1] = out;
+        src[0] = in;
+        for (int i = 1; i < np; ++i) src[i] = dst[i - 1];
+    };
+    bool need_ws = true;
+    route(true, nullptr);
+    if (np == 2 && (const void *)in != (const void *)out) need_ws = false;
+    if (need_ws) {
+        int st = ws.ensure(bytes, why);
+        if (st != GBFFT_OK) return st;
+        float2 *w = (float2 *)ws.ptr;
+        route(true, w);
+        if ((const void *)src[0] == (const void *)dst[0]) route(false, w);
+    }
+    const bool inv = direction == GBFFT_INVERSE;
+    const float scale = inv ? ldexpf(1.0f, -p.logn) : 1.0f;
+    for (int i = 0; i < np; ++i) {
+        const PassDesc &d = p.passes[i];
+        const float in_im = (i == 0 && inv) ? -1.0f : 1.0f;
+        const float out_re = (i == np - 1) ? scale : 1.0f;
+        const float out_im = (i == np - 1 && inv) ? -scale : 1.0f;
+        e = pass_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
+                        p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, stream);
+        if (e != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        ++launches;
+    }
+    return GBFFT_OK;
+}
+
+}  // namespace gbfft

@@ -1,0 +1,62 @@
+// Plan = everything size-specific the transform needs, built once per log2 N
+// and cached by the context.  Replaces the reference's SizeCache
+// (larsjoost/wgls-rs-fft src/lib.rs:230-259, 709-943): instead of wgpu buffers,
+// bind groups and per-stage uniforms it holds device twiddle tables and the
+// kernel schedule (single pass, or a list of global passes for N > 2^14).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "gbfft_internal.h"
+
+namespace gbfft {
+
+struct DeviceBuffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want, std::string &err);
+    void release();
+    ~DeviceBuffer() { release(); }
+};
+
+// One global Stockham pass of the multi-pass form (fft_passes.cu).
+struct PassDesc {
+    const void *fn = nullptr;
+    int logr = 0;        // transform size handled in shared memory: R = 2^logr
+    int logp = 0;        // product of the radices of earlier global passes
+    int cols = 0;        // columns (independent length-R DFTs) per CTA
+    int threads = 0;
+    size_t smem = 0;
+    uint64_t sub_tw_offset = 0;  // this pass's in-SMEM sub-pass tables
+};
+
+struct Plan {
+    int logn = 0;
+    bool multipass = false;
+    bool needs_workspace = false;
+    RowsKernelInfo rows;
+    std::vector<PassDesc> passes;
+    // twiddle table (device): rows sub-pass tables, or for multi-pass the
+    // per-pass sub-pass tables followed by the two-level W_N table.
+    float2 *tw = nullptr;
+    uint64_t tw_entries = 0;
+    uint64_t tw_lo_offset = 0, tw_hi_offset = 0;  // W_N^i (i < 2^s), W_N^{i 2^s}
+    int tw_split = 0;                             // s
+    ~Plan();
+};
+
+// fft_passes.cu
+bool pass_kernel_info(int logr, bool first, PassDesc &d, std::vector<int> &sub_logr, std::vector<int> &sub_logp);
+cudaError_t pass_prepare(const PassDesc &d);
+cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
+                        const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
+                        float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream);
+
+// log2 radices of the global passes for a multi-pass transform of 2^logn.
+std::vector<int> split_passes(int logn);
+
+int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why);
+int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,
+                 DeviceBuffer &ws, cudaStream_t stream, uint64_t &launches, std::string &why);
+
+}  // namespace gbfft

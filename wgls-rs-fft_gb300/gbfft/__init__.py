@@ -1,0 +1,17 @@
+"""gbfft: GB300-native batched power-of-two C2C FFT (Python side of the C ABI).
+
+The transform itself lives in libgbfft.so (CUDA, sm_103a); this package only
+builds and binds it.  Import it with ``wgls-rs-fft_gb300`` on sys.path.
+"""
+from ._lib import (ERR_CUDA, ERR_INVALID_ARGUMENT, ERR_INVALID_SIZE, ERR_LENGTH_MISMATCH, ERR_NO_DEVICE,
+                   ERR_OUT_OF_MEMORY, ERR_TIMEOUT, ERR_UNSUPPORTED, FORWARD, INVERSE, OK, PREC_FP32, SIGNATURES,
+                   Context, GbfftError, is_available, lib_path, load, status_string)
+from .build import LIB_PATH, build
+from .gpu_fft import FftExecutor, GpuFft
+
+__all__ = [
+    "Context", "GbfftError", "GpuFft", "FftExecutor", "FORWARD", "INVERSE", "PREC_FP32", "OK",
+    "ERR_INVALID_SIZE", "ERR_LENGTH_MISMATCH", "ERR_INVALID_ARGUMENT", "ERR_NO_DEVICE", "ERR_OUT_OF_MEMORY",
+    "ERR_CUDA", "ERR_TIMEOUT", "ERR_UNSUPPORTED", "SIGNATURES", "build", "load", "lib_path", "LIB_PATH",
+    "is_available", "status_string",
+]

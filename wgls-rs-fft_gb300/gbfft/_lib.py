@@ -1,0 +1,178 @@
+"""ctypes binding of the C ABI in include/gbfft.h.
+
+There is no fallback: if libgbfft.so is missing or cannot be loaded, every
+entry point raises.  The library is the only implementation of the transform.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from .build import LIB_PATH
+
+FORWARD = -1
+INVERSE = +1
+PREC_FP32 = 0
+
+OK = 0
+ERR_INVALID_SIZE = 1
+ERR_LENGTH_MISMATCH = 2
+ERR_INVALID_ARGUMENT = 3
+ERR_NO_DEVICE = 4
+ERR_OUT_OF_MEMORY = 5
+ERR_CUDA = 6
+ERR_TIMEOUT = 7
+ERR_UNSUPPORTED = 8
+
+# Every symbol include/gbfft.h declares, with (restype, argtypes).
+_vp = ctypes.c_void_p
+_u64 = ctypes.c_uint64
+_int = ctypes.c_int
+_fp = ctypes.POINTER(ctypes.c_float)
+SIGNATURES = {
+    "gbfft_is_available": (_int, []),
+    "gbfft_create": (_int, [_int, ctypes.POINTER(_vp)]),
+    "gbfft_destroy": (None, [_vp]),
+    "gbfft_last_error": (ctypes.c_char_p, [_vp]),
+    "gbfft_status_string": (ctypes.c_char_p, [_int]),
+    "gbfft_c2c_host": (_int, [_vp, _vp, _vp, _u64, _u64, _int]),
+    "gbfft_c2c_host_rows": (_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_u64), ctypes.POINTER(_vp), _u64, _int]),
+    "gbfft_c2c_device": (_int, [_vp, _vp, _vp, _u64, _u64, _int, _vp]),
+    "gbfft_bench_device": (_int, [_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(ctypes.c_double)]),
+    "gbfft_set_precision": (_int, [_vp, _int]),
+    "gbfft_launch_count": (_u64, [_vp]),
+    "gbfft_version": (ctypes.c_char_p, []),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class GbfftError(RuntimeError):
+    """A non-zero gbfft status; str() is the library's message."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+def lib_path() -> str:
+    return os.environ.get("GBFFT_LIB", LIB_PATH)
+
+
+def load():
+    """Load libgbfft.so (raises if it is absent -- there is no CPU path)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = lib_path()
+            if not os.path.exists(path):
+                raise RuntimeError(f"libgbfft.so not built ({path}); run gbfft.build.build()")
+            L = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+        return _lib
+
+
+def status_string(status: int) -> str:
+    return load().gbfft_status_string(status).decode()
+
+
+def is_available() -> bool:
+    return bool(load().gbfft_is_available())
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return int(a)
+
+
+class Context:
+    """Owns one gbfft_ctx (one device, one stream, a plan cache)."""
+
+    def __init__(self, device: int = 0):
+        self._L = load()
+        h = _vp()
+        st = self._L.gbfft_create(device, ctypes.byref(h))
+        if st != OK:
+            raise GbfftError(st, status_string(st))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gbfft_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def last_error(self) -> str:
+        return self._L.gbfft_last_error(self._h).decode()
+
+    def _check(self, st: int):
+        if st != OK:
+            msg = self.last_error() or status_string(st)
+            raise GbfftError(st, msg)
+
+    def launch_count(self) -> int:
+        return int(self._L.gbfft_launch_count(self._h))
+
+    def set_precision(self, precision: int):
+        self._check(self._L.gbfft_set_precision(self._h, precision))
+
+    def c2c_host(self, x: np.ndarray, direction: int = FORWARD, out: np.ndarray | None = None) -> np.ndarray:
+        """Transform a [batch, n] complex64 host array (contiguous); returns out."""
+        x = np.ascontiguousarray(x, dtype=np.complex64)
+        if x.ndim == 1:
+            x = x[None, :]
+        if out is None:
+            out = np.empty_like(x)
+        b, n = x.shape
+        self._check(self._L.gbfft_c2c_host(self._h, _ptr(x), _ptr(out), n, b, direction))
+        return out
+
+    def c2c_host_ptr(self, in_ptr: int, out_ptr: int, n: int, batch: int, direction: int):
+        self._check(self._L.gbfft_c2c_host(self._h, in_ptr, out_ptr, n, batch, direction))
+
+    def c2c_host_rows(self, rows, direction: int = FORWARD):
+        """The reference's argument shape: a list of 1-D complex64 rows."""
+        rows = [np.ascontiguousarray(r, dtype=np.complex64) for r in rows]
+        outs = [np.empty_like(r) for r in rows]
+        b = len(rows)
+        in_p = (_vp * max(b, 1))(*[r.ctypes.data for r in rows])
+        out_p = (_vp * max(b, 1))(*[o.ctypes.data for o in outs])
+        lens = (_u64 * max(b, 1))(*[r.size for r in rows])
+        self._check(self._L.gbfft_c2c_host_rows(self._h, in_p, lens, out_p, b, direction))
+        return outs
+
+    def c2c_device(self, d_in, d_out, n: int, batch: int, direction: int = FORWARD, stream=None):
+        """Enqueue on device pointers (ints or tensors); stream is a cudaStream_t int."""
+        s = 0 if stream is None else int(stream)
+        self._check(self._L.gbfft_c2c_device(self._h, _ptr(d_in), _ptr(d_out), n, batch, direction, s or None))
+
+    def bench_device(self, n: int, batch: int, direction: int = FORWARD, warmup: int = 3, iters: int = 20) -> float:
+        sec = ctypes.c_double()
+        self._check(self._L.gbfft_bench_device(self._h, n, batch, direction, warmup, iters, ctypes.byref(sec)))
+        return sec.value

@@ -1,0 +1,146 @@
+"""Seeded synthetic signals for the benchmark workloads and the parity tests.
+
+Counter-based generator built on the PCG hash of the reference's noise stage
+(larsjoost/wgls-rs-fft examples/parallel_pipeline.rs:36-40):
+
+    pcg(v):   s = v * 747796405 + 2891336453
+              w = ((s >> ((s >> 28) + 4)) ^ s) * 277803737
+              return (w >> 22) ^ w                      (all u32, wrapping)
+    h(stream, seed, i) = pcg(pcg(seed ^ stream * 0x9E3779B9) + i)
+
+Element i of a [batch, n] array is i = row * n + col (u32).  Real parts use
+stream 0, imaginary parts stream 1.
+
+    uniform[-1, 1):  ((h >> 8) * 2^-24) * 2 - 1          (exact in f32)
+    normal N(0, 1):  Box-Muller in FP64 from u1 = ((h0 >> 8) + 1) 2^-24 in (0, 1]
+                     and u2 = (h1 >> 8) 2^-24, rounded once to f32:
+                     (r cos 2 pi u2, r sin 2 pi u2), r = sqrt(-2 ln u1)
+
+numpy (host) and torch (device) versions produce identical integers; the
+uniform path is bit-identical, the normal path may differ in the last f32 ulp
+only where the host and device libm round a double differently.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_M32 = 0xFFFFFFFF
+GOLDEN = 0x9E3779B9
+
+
+def pcg_np(v: np.ndarray) -> np.ndarray:
+    v = v.astype(np.uint32, copy=False)
+    with np.errstate(over="ignore"):
+        s = v * np.uint32(747796405) + np.uint32(2891336453)
+        w = ((s >> ((s >> np.uint32(28)) + np.uint32(4))) ^ s) * np.uint32(277803737)
+    return (w >> np.uint32(22)) ^ w
+
+
+def stream_key(stream: int, seed: int) -> int:
+    k = np.array([(seed ^ ((stream * GOLDEN) & _M32)) & _M32], dtype=np.uint32)
+    return int(pcg_np(k)[0])
+
+
+def hash_np(stream: int, seed: int, idx: np.ndarray) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        return pcg_np(np.uint32(stream_key(stream, seed)) + idx.astype(np.uint32, copy=False))
+
+
+def _chunks(total: int, chunk: int = 1 << 24):
+    for a in range(0, total, chunk):
+        yield a, min(total, a + chunk)
+
+
+def uniform_c64(batch: int, n: int, seed: int) -> np.ndarray:
+    """[batch, n] complex64, re/im iid uniform[-1, 1)."""
+    total = batch * n
+    out = np.empty(total, dtype=np.complex64)
+    f = out.view(np.float32)
+    for a, b in _chunks(total):
+        idx = np.arange(a, b, dtype=np.uint64).astype(np.uint32)
+        for st in (0, 1):
+            h = hash_np(st, seed, idx)
+            f[2 * a + st:2 * b:2] = ((h >> np.uint32(8)).astype(np.float32) * np.float32(2.0 ** -24)) * np.float32(2.0) - np.float32(1.0)
+    return out.reshape(batch, n)
+
+
+def normal_c64(batch: int, n: int, seed: int) -> np.ndarray:
+    """[batch, n] complex64, re/im iid N(0, 1) (Box-Muller pair per sample)."""
+    total = batch * n
+    out = np.empty(total, dtype=np.complex64)
+    f = out.view(np.float32)
+    for a, b in _chunks(total):
+        idx = np.arange(a, b, dtype=np.uint64).astype(np.uint32)
+        h0 = hash_np(0, seed, idx)
+        h1 = hash_np(1, seed, idx)
+        u1 = ((h0 >> np.uint32(8)).astype(np.float64) + 1.0) * 2.0 ** -24
+        u2 = (h1 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24
+        r = np.sqrt(-2.0 * np.log(u1))
+        ang = 2.0 * np.pi * u2
+        f[2 * a:2 * b:2] = (r * np.cos(ang)).astype(np.float32)
+        f[2 * a + 1:2 * b:2] = (r * np.sin(ang)).astype(np.float32)
+    return out.reshape(batch, n)
+
+
+def sin_row(n: int) -> np.ndarray:
+    """x_i = sin(0.1 i) + 0j with 0.1*i rounded in f32 first (the reference's
+    test signal form (i as f32 * 0.1).sin(), tests/gpu_fft_test.rs:8-15)."""
+    arg = np.arange(n, dtype=np.float32) * np.float32(0.1)
+    return np.sin(arg.astype(np.float64)).astype(np.float32).astype(np.complex64)
+
+
+def hann_window(n: int) -> np.ndarray:
+    """w_i = 0.5 (1 - cos(2 pi i / (n - 1))) in FP64, rounded to f32
+    (tests/test_utils.rs:39-48 computes the same formula in f32)."""
+    if n == 1:
+        return np.ones(1, dtype=np.float32)
+    i = np.arange(n, dtype=np.float64)
+    return (0.5 * (1.0 - np.cos(2.0 * np.pi * i / (n - 1)))).astype(np.float32)
+
+
+# ---- device (torch) versions: same integers, generated in HBM ------------
+
+def _pcg_torch(v):
+    import torch
+    m = 0xFFFFFFFF
+    s = (v * 747796405 + 2891336453) & m
+    w = ((torch.bitwise_right_shift(s, (s >> 28) + 4) ^ s) * 277803737) & m
+    return ((w >> 22) ^ w) & m
+
+
+def _hash_torch(stream, seed, idx):
+    return _pcg_torch((idx + stream_key(stream, seed)) & 0xFFFFFFFF)
+
+
+def normal_c64_torch(batch: int, n: int, seed: int, device="cuda"):
+    """Device-side normal_c64 (complex64 tensor [batch, n])."""
+    import torch
+    total = batch * n
+    out = torch.empty(total, 2, dtype=torch.float32, device=device)
+    step = 1 << 24
+    for a in range(0, total, step):
+        b = min(total, a + step)
+        idx = torch.arange(a, b, dtype=torch.int64, device=device)
+        h0 = _hash_torch(0, seed, idx)
+        h1 = _hash_torch(1, seed, idx)
+        u1 = ((h0 >> 8).to(torch.float64) + 1.0) * 2.0 ** -24
+        u2 = (h1 >> 8).to(torch.float64) * 2.0 ** -24
+        r = torch.sqrt(-2.0 * torch.log(u1))
+        ang = 2.0 * np.pi * u2
+        out[a:b, 0] = (r * torch.cos(ang)).to(torch.float32)
+        out[a:b, 1] = (r * torch.sin(ang)).to(torch.float32)
+    return torch.view_as_complex(out).reshape(batch, n)
+
+
+def uniform_c64_torch(batch: int, n: int, seed: int, device="cuda"):
+    import torch
+    total = batch * n
+    out = torch.empty(total, 2, dtype=torch.float32, device=device)
+    step = 1 << 24
+    for a in range(0, total, step):
+        b = min(total, a + step)
+        idx = torch.arange(a, b, dtype=torch.int64, device=device)
+        for st in (0, 1):
+            h = _hash_torch(st, seed, idx)
+            out[a:b, st] = ((h >> 8).to(torch.float32) * 2.0 ** -24) * 2.0 - 1.0
+    return torch.view_as_complex(out).reshape(batch, n)

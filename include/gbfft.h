@@ -93,8 +93,8 @@ int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows,
 /* Device-resident entry point (new; no reference counterpart -- the reference
  * always round-trips through host memory).  `d_in`/`d_out` are device
  * pointers to batch*n interleaved complex<f32>; they may alias.  Work is
- * enqueued on `stream` (a cudaStream_t; NULL selects the context's stream)
- * and the call returns without synchronising. */
+ * enqueued on `stream` (a cudaStream_t; NULL is the CUDA default stream, as
+ * everywhere in CUDA) and the call returns without synchronising. */
 int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,
                      uint64_t batch, int direction, void *stream);
 

@@ -111,6 +111,9 @@ int get_plan(gbfft_ctx *ctx, int logn, Plan **out) {
     std::string why;
     int st = plan_build(*p, logn, ctx->stream, why);
     if (st != GBFFT_OK) return fail(ctx, st, "plan for N=2^%d: %s", logn, why.c_str());
+    // Tables are filled on the context's stream; transforms may run on any
+    // stream, so finish the fill before the plan is used (once per size).
+    GB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     *out = p.get();
     ctx->plans[logn] = std::move(p);
     return GBFFT_OK;
@@ -232,8 +235,7 @@ int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n, 
     if (batch == 0) return GBFFT_OK;
     if (!d_in || !d_out) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null device pointer");
     GB_CUDA(ctx, cudaSetDevice(ctx->device));
-    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
-    return run_device(ctx, (const float2 *)d_in, (float2 *)d_out, n, batch, direction, s);
+    return run_device(ctx, (const float2 *)d_in, (float2 *)d_out, n, batch, direction, (cudaStream_t)stream);
 }
 
 // Host batch already contiguous in `in` (pinned or pageable).

@@ -168,7 +168,8 @@ class Context:
         return outs
 
     def c2c_device(self, d_in, d_out, n: int, batch: int, direction: int = FORWARD, stream=None):
-        """Enqueue on device pointers (ints or tensors); stream is a cudaStream_t int."""
+        """Enqueue on device pointers (ints or tensors).  `stream` is a
+        cudaStream_t as an int; None or 0 is the CUDA default stream."""
         s = 0 if stream is None else int(stream)
         self._check(self._L.gbfft_c2c_device(self._h, _ptr(d_in), _ptr(d_out), n, batch, direction, s or None))
 

@@ -98,6 +98,24 @@ int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows,
 int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,
                      uint64_t batch, int direction, void *stream);
 
+/* Allocation-free variant of gbfft_c2c_device (no counterpart in the
+ * reference).  For callers that may not allocate GPU memory -- code running in
+ * a host callback or an allocator hook, under a memory pool that owns all of
+ * the device's memory, or on a latency path where cudaMalloc/cudaFree and the
+ * synchronisation they imply are not acceptable.  It never calls cudaMalloc,
+ * cudaFree or any allocating routine, and it needs no context.
+ *
+ * Limits: n a power of two with 2^15 <= n <= 2^20 and n * batch <= 2^22
+ * (the library's built-in 32 MiB scratch array); anything larger or smaller
+ * returns GBFFT_ERR_UNSUPPORTED, a non-power-of-two n GBFFT_ERR_INVALID_SIZE.
+ * Device pointers and stream as for gbfft_c2c_device; runs on the current
+ * device.  The first call on each device sets up (looks up the scratch and
+ * twiddle arrays and fills the tables) and synchronises `stream`: make that
+ * first call before any stream capture.  All calls on a device share the one
+ * scratch array, so calls that overlap on the GPU race: serialise them. */
+int gbfft_c2c_device_noalloc(const void *d_in, void *d_out, uint64_t n,
+                             uint64_t batch, int direction, void *stream);
+
 /* Replaces GpuFftTrait::benchmark_gpu_only (src/lib.rs:108-156, 673-707):
  * device-only timing of `iters` transforms of an n x batch device batch after
  * `warmup` untimed ones, with CUDA events on the context's stream.  Writes the

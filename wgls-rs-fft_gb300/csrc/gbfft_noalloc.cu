@@ -1,0 +1,152 @@
+// gbfft_c2c_device_noalloc: the two-pass transform (N = 2^15 .. 2^20) for
+// callers that cannot allocate GPU memory.
+//
+// Who needs it: code that runs where cudaMalloc is off limits -- inside a host
+// callback or another library's allocator hook, in a process whose device
+// memory is fully reserved by a pool it does not own, or in real-time paths
+// where an allocation (and the implicit synchronisation cudaFree brings) would
+// stall.  The regular entry points allocate on first use of a size (twiddle
+// tables, a workspace); this one never calls cudaMalloc, cudaFree or any
+// allocating library routine.
+//
+// Where its memory comes from: two file-scope device arrays of this library,
+// a 32 MiB scratch buffer for the intermediate result between the two global
+// passes, and a 256 KiB table area for the twiddles of every supported size.
+// The driver reserves them when it loads this library's code on a GPU; every
+// GPU that loads the library holds them until the process exits.
+//
+// Set-up: the first call on each device (with that device current) looks up
+// the arrays' device addresses with cudaGetSymbolAddress, fills the twiddle
+// tables for all supported sizes and synchronises the caller's stream.  Make
+// that first call before any stream capture.  Later calls only enqueue the two
+// pass kernels on the caller's stream.
+//
+// Sharing: every call on a device uses the same scratch array, which keeps
+// whatever the previous call left in it.  Nothing in it needs to start at
+// zero (the first pass overwrites every sample the second pass reads).  Calls
+// that overlap on the GPU (different streams, or concurrent host threads) race
+// on the scratch array: serialise them.
+#include <mutex>
+#include <vector>
+
+#include "gbfft_internal.h"
+#include "gbfft_plan.h"
+
+namespace gbfft {
+namespace {
+
+constexpr int kNaMinLogN = 15;
+constexpr int kNaMaxLogN = 20;
+constexpr uint64_t kNaScratchSamples = 1ull << 22;  // 32 MiB of complex<f32>
+constexpr uint64_t kNaTwiddleEntries = 1ull << 15;  // 256 KiB
+constexpr int kNaMaxDevices = 64;
+
+static __device__ __align__(256) float2 g_na_scratch[kNaScratchSamples];
+static __device__ __align__(256) float2 g_na_twiddles[kNaTwiddleEntries];
+
+struct NaPlan {
+    PassDesc pass[2];
+    uint64_t lo_off = 0, hi_off = 0;
+    int split = 0;
+};
+
+struct NaDevice {
+    bool ready = false;
+    float2 *scratch = nullptr;
+    float2 *tw = nullptr;
+    NaPlan plan[kNaMaxLogN + 1];
+};
+
+NaDevice g_na_dev[kNaMaxDevices];
+std::mutex g_na_mu;
+
+int na_setup(int dev, cudaStream_t stream, NaDevice &d) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_na_scratch) != cudaSuccess) {
+        cudaGetLastError();
+        return GBFFT_ERR_CUDA;
+    }
+    d.scratch = (float2 *)p;
+    if (cudaGetSymbolAddress(&p, g_na_twiddles) != cudaSuccess) {
+        cudaGetLastError();
+        return GBFFT_ERR_CUDA;
+    }
+    d.tw = (float2 *)p;
+    uint64_t off = 0;
+    for (int L = kNaMinLogN; L <= kNaMaxLogN; ++L) {
+        std::vector<int> parts = split_passes(L);
+        if (parts.size() != 2) return GBFFT_ERR_UNSUPPORTED;
+        std::vector<TwiddleSegment> segs;
+        NaPlan &np = d.plan[L];
+        int logp = 0;
+        for (int i = 0; i < 2; ++i) {
+            std::vector<int> lr, lp;
+            if (!pass_kernel_info(parts[i], i == 0, np.pass[i], lr, lp)) return GBFFT_ERR_UNSUPPORTED;
+            if (pass_prepare(np.pass[i]) != cudaSuccess) return GBFFT_ERR_CUDA;
+            np.pass[i].logp = logp;
+            np.pass[i].sub_tw_offset = off;
+            for (size_t s = 1; s < lr.size(); ++s) {
+                TwiddleSegment seg = {off, (uint64_t)((1 << lr[s]) - 1) << lp[s], 0, lr[s] + lp[s], lp[s], 0};
+                segs.push_back(seg);
+                off += seg.count;
+            }
+            logp += parts[i];
+        }
+        np.split = (L + 1) / 2;
+        np.lo_off = off;
+        segs.push_back({off, 1ull << np.split, 1, L, 0, 0});
+        off += 1ull << np.split;
+        np.hi_off = off;
+        segs.push_back({off, 1ull << (L - np.split), 1, L, 0, np.split});
+        off += 1ull << (L - np.split);
+        if (off > kNaTwiddleEntries) return GBFFT_ERR_UNSUPPORTED;
+        if (twiddle_fill(d.tw, segs.data(), (int)segs.size(), stream) != cudaSuccess) return GBFFT_ERR_CUDA;
+    }
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return GBFFT_ERR_CUDA;
+    d.ready = true;
+    (void)dev;
+    return GBFFT_OK;
+}
+
+}  // namespace
+}  // namespace gbfft
+
+using namespace gbfft;
+
+extern "C" int gbfft_c2c_device_noalloc(const void *d_in, void *d_out, uint64_t n, uint64_t batch, int direction,
+                                        void *stream) {
+    if (direction != GBFFT_FORWARD && direction != GBFFT_INVERSE) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (n == 0 || (n & (n - 1)) != 0) return GBFFT_ERR_INVALID_SIZE;
+    int L = 0;
+    while ((1ull << L) < n) ++L;
+    if (L < kNaMinLogN || L > kNaMaxLogN) return GBFFT_ERR_UNSUPPORTED;
+    if (batch == 0) return GBFFT_OK;
+    if (batch > kNaScratchSamples / n) return GBFFT_ERR_UNSUPPORTED;  // n * batch <= 2^22
+    if (!d_in || !d_out) return GBFFT_ERR_INVALID_ARGUMENT;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) {
+        cudaGetLastError();
+        return GBFFT_ERR_NO_DEVICE;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    NaDevice &d = g_na_dev[dev];
+    {
+        std::lock_guard<std::mutex> lock(g_na_mu);
+        if (!d.ready) {
+            int st = na_setup(dev, s, d);
+            if (st != GBFFT_OK) return st;
+        }
+    }
+    const NaPlan &np = d.plan[L];
+    const bool inv = direction == GBFFT_INVERSE;
+    const float scale = inv ? ldexpf(1.0f, -L) : 1.0f;
+    // pass 0: input -> scratch (conjugate on load for the inverse)
+    cudaError_t e = pass_launch(np.pass[0], (const float2 *)d_in, d.scratch, batch, L, d.tw + np.pass[0].sub_tw_offset,
+                                d.tw + np.lo_off, d.tw + np.hi_off, np.split, inv ? -1.0f : 1.0f, 1.0f, 1.0f, s);
+    if (e != cudaSuccess) return GBFFT_ERR_CUDA;
+    // pass 1: scratch -> output (conjugate and scale by 1/N on store for the inverse)
+    e = pass_launch(np.pass[1], d.scratch, (float2 *)d_out, batch, L, d.tw + np.pass[1].sub_tw_offset,
+                    d.tw + np.lo_off, d.tw + np.hi_off, np.split, 1.0f, scale, inv ? -scale : 1.0f, s);
+    if (e != cudaSuccess) return GBFFT_ERR_CUDA;
+    return GBFFT_OK;
+}

@@ -41,6 +41,7 @@ SIGNATURES = {
     "gbfft_c2c_host": (_int, [_vp, _vp, _vp, _u64, _u64, _int]),
     "gbfft_c2c_host_rows": (_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_u64), ctypes.POINTER(_vp), _u64, _int]),
     "gbfft_c2c_device": (_int, [_vp, _vp, _vp, _u64, _u64, _int, _vp]),
+    "gbfft_c2c_device_noalloc": (_int, [_vp, _vp, _u64, _u64, _int, _vp]),
     "gbfft_bench_device": (_int, [_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_set_precision": (_int, [_vp, _int]),
     "gbfft_launch_count": (_u64, [_vp]),

@@ -46,6 +46,8 @@ WORKLOADS = {
     "n8192_b8192": (13, 8192, "normal", 2),
     "n16384_b4096": (14, 4096, "normal", 2),
     "n65536_b4096": (16, 4096, "normal", 2),
+    "n65536_b1024": (16, 1024, "normal", 2),
+    "n262144_b256": (18, 256, "normal", 2),
     "n4194304_b64": (22, 64, "normal", 3),
     "n16777216_b4": (24, 4, "normal", 3),
     "n67108864_b1": (26, 1, "normal", 3),

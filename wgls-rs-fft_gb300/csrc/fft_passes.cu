@@ -15,8 +15,11 @@
 // column's R outputs contiguously; it stages them through shared memory
 // (XOR-swizzled [column][row]) so that its HBM stores are fully coalesced too.
 //
-// The pre-twiddle W_{R p}^{m k} = W_N^{(m k) N/(R p)} comes from two FP64-built
-// tables (W_N^i for i < 2^s and W_N^{i 2^s}), one complex multiply each.
+// Pre-twiddle: thread t of column j holds rows m = t + T e, and
+//   W_{R p}^{m k} = W_{R p}^{t k} * W_{E p}^{e k}.
+// The first factor is one lookup per thread; the second depends only on the
+// column and e, so the CTA builds it once into a padded 16 x 17 shared table.
+// Both come from two FP64-built tables (W_N^i for i < 2^s and W_N^{i 2^s}).
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"
 #include "fft_smem.cuh"
@@ -31,7 +34,8 @@ struct PassCfg : SubCfg<LOGR> {
     using S = SubCfg<LOGR>;
     static constexpr int THREADS = kPassCols * S::T;
     static constexpr int MINB = THREADS >= 1024 ? 1 : 1024 / THREADS;
-    static constexpr size_t SMEM = (size_t)kPassCols * S::N * sizeof(float2);
+    static constexpr int COLTW_STRIDE = S::E + 1;  // padded: conflict-free column reads
+    static constexpr size_t SMEM = ((size_t)kPassCols * S::N + kPassCols * COLTW_STRIDE) * sizeof(float2);
 };
 
 template <int LOGR, int I, bool DONE = (I >= SubCfg<LOGR>::NSUB)>
@@ -48,7 +52,7 @@ struct PassChain {
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < C::E; ++e) v[e] = buf[((t + C::T * e) << kPassLogCols) + c];
-        subpass_compute<C::LOGE, C::logr(I), C::logp(I), C::LOGT>(v, t, tw + C::tw_offset(I));
+        subpass_run<LOGR, I>(v, t, tw);
         PassChain<LOGR, I + 1>::run(v, t, c, buf, tw);
     }
 };
@@ -56,6 +60,11 @@ template <int LOGR, int I>
 struct PassChain<LOGR, I, true> {
     __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR>::E], int, int, float2 *, const float2 *) {}
 };
+
+__device__ __forceinline__ float2 twiddle_2level(const float2 *__restrict__ lo, const float2 *__restrict__ hi,
+                                                 uint32_t ex, int split) {
+    return cmul(ld_tw(hi + (ex >> split)), ld_tw(lo + (ex & ((1u << split) - 1))));
+}
 
 template <int LOGR, bool FIRST>
 __global__ void __launch_bounds__(PassCfg<LOGR>::THREADS, PassCfg<LOGR>::MINB)
@@ -65,6 +74,7 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
     using C = PassCfg<LOGR>;
     constexpr int R = C::N, T = C::T, E = C::E;
     extern __shared__ float2 smem_pass[];
+    float2 *coltw = smem_pass + kPassCols * R;
     const int tid = threadIdx.x;
     const int c = tid & (kPassCols - 1);
     const int t = tid >> kPassLogCols;
@@ -85,18 +95,22 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
         v[e] = x;
     }
     if (!FIRST) {
-        const uint32_t k = j & ((1u << logp) - 1);
-        const int sh = logn - LOGR - logp;
-        const uint32_t lo_mask = (1u << tw_split) - 1;
-#pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const uint32_t m = t + T * e;
-            const uint32_t ex = (m * k) << sh;
-            const float2 w = cmul(ld_tw(tw_hi + (ex >> tw_split)), ld_tw(tw_lo + (ex & lo_mask)));
-            v[e] = cmul(v[e], w);
+        const uint32_t pmask = (1u << logp) - 1;
+        // per-column factors W_{E p}^{e k} = W_N^{(e k) << (logn - LOGE - logp)}
+        const int sh_col = logn - C::LOGE - logp;
+        for (int i = tid; i < kPassCols * E; i += C::THREADS) {
+            const int cc = i >> C::LOGE, ee = i & (E - 1);
+            const uint32_t kk = (j0 + cc) & pmask;
+            coltw[cc * C::COLTW_STRIDE + ee] = twiddle_2level(tw_lo, tw_hi, (kk * ee) << sh_col, tw_split);
         }
+        // per-thread factor W_{R p}^{t k}
+        const uint32_t k = j & pmask;
+        const float2 a = twiddle_2level(tw_lo, tw_hi, (t * k) << (logn - LOGR - logp), tw_split);
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = cmul(v[e], cmul(a, coltw[c * C::COLTW_STRIDE + e]));
     }
-    subpass_compute<C::LOGE, C::logr(0), 0, C::LOGT>(v, t, tw);
+    subpass_run<LOGR, 0>(v, t, tw);
     PassChain<LOGR, 1>::run(v, t, c, smem_pass, tw);
 
     constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
@@ -140,25 +154,21 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
 // ---------------------------------------------------------------------------
 
 template <int LOGR>
-static void pass_describe(PassDesc &d, bool first, std::vector<int> &sub_logr, std::vector<int> &sub_logp) {
+static void pass_describe(PassDesc &d, bool first) {
     using C = PassCfg<LOGR>;
     d.fn = first ? (const void *)fft_pass_kernel<LOGR, true> : (const void *)fft_pass_kernel<LOGR, false>;
     d.threads = C::THREADS;
     d.smem = C::SMEM;
     d.cols = kPassCols;
-    sub_logr.clear();
-    sub_logp.clear();
-    for (int i = 0; i < C::NSUB; ++i) {
-        sub_logr.push_back(C::logr(i));
-        sub_logp.push_back(C::logp(i));
-    }
+    d.nseg = subcfg_segments<LOGR>(d.segs, 0);
+    d.tw_entries = C::tw_entries();
 }
 
-bool pass_kernel_info(int logr, bool first, PassDesc &d, std::vector<int> &sub_logr, std::vector<int> &sub_logp) {
+bool pass_kernel_info(int logr, bool first, PassDesc &d) {
     d.logr = logr;
     switch (logr) {
 #define GBFFT_PASS_CASE(L) \
-    case L: pass_describe<L>(d, first, sub_logr, sub_logp); return true;
+    case L: pass_describe<L>(d, first); return true;
         GBFFT_PASS_CASE(5) GBFFT_PASS_CASE(6) GBFFT_PASS_CASE(7) GBFFT_PASS_CASE(8)
         GBFFT_PASS_CASE(9) GBFFT_PASS_CASE(10)
 #undef GBFFT_PASS_CASE

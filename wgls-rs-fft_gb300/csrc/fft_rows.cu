@@ -50,7 +50,7 @@ struct RowsChain {
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < C::E; ++e) v[e] = buf[swz(t + C::T * e, PP)];
-        subpass_compute<C::LOGE, C::logr(I), C::logp(I), C::LOGT>(v, t, tw + C::tw_offset(I));
+        subpass_run<LOGN, I>(v, t, tw);
         RowsChain<LOGN, I + 1>::run(v, t, buf, tw);
     }
 };
@@ -81,7 +81,7 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
         x.y *= in_im_sign;
         v[e] = x;
     }
-    subpass_compute<C::LOGE, C::logr(0), 0, C::LOGT>(v, t, tw);
+    subpass_run<LOGN, 0>(v, t, tw);
     RowsChain<LOGN, 1>::run(v, t, buf, tw);
 
     // Last sub-pass (p * R = N): output q of butterfly j sits at j + q p.
@@ -110,11 +110,7 @@ static void rows_describe(RowsKernelInfo &k) {
     k.threads = C::THREADS;
     k.transforms_per_cta = C::G;
     k.smem = C::SMEM;
-    k.nsub = C::NSUB;
-    for (int i = 0; i < C::NSUB; ++i) {
-        k.sub_logr[i] = C::logr(i);
-        k.sub_logp[i] = C::logp(i);
-    }
+    k.nseg = subcfg_segments<LOGN>(k.segs, 0);
     k.tw_entries = C::tw_entries();
 }
 

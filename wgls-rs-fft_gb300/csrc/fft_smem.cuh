@@ -12,7 +12,10 @@
 // sub-pass of radix R it runs E/R butterflies j = t + T b, butterfly b using
 // register slots b + m E/R.
 #pragma once
+#include <utility>
+
 #include "fft_core.cuh"
+#include "gbfft_internal.h"
 
 namespace gbfft {
 
@@ -30,36 +33,107 @@ struct SubCfg {
     // log2 radix of sub-pass i and log2 of p = product of earlier radices
     __host__ __device__ static constexpr int logr(int i) { return i < NFULL ? LOGE : LREM; }
     __host__ __device__ static constexpr int logp(int i) { return i * LOGE; }
-    // Offset (complex entries) of sub-pass i's table in the concatenation of
-    // the tables of sub-passes 1..NSUB-1.  Table of sub-pass i holds
-    // W_{R p}^{m k} for m in [1, R), k in [0, p), laid out [m-1][k].
+    // The last sub-pass with radix R < E runs E/R butterflies per thread with
+    // k = j = t + T b; its twiddle W_N^{m (t + T b)} factors into a table entry
+    // W_N^{m t} and the constant W_E^{m b}.
+    __host__ __device__ static constexpr bool factored(int i) { return i > 0 && logr(i) < LOGE; }
+    // Table of sub-pass i (i >= 1): entries W_M^{m k}, m in [1, R), k in
+    // [0, 2^tw_logp(i)), laid out [m-1][k], M = 2^tw_logm(i).
+    __host__ __device__ static constexpr int tw_logp(int i) { return factored(i) ? LOGT : logp(i); }
+    __host__ __device__ static constexpr int tw_logm(int i) { return factored(i) ? LOGN : logr(i) + logp(i); }
+    __host__ __device__ static constexpr int tw_count(int i) { return ((1 << logr(i)) - 1) << tw_logp(i); }
     __host__ __device__ static constexpr int tw_offset(int i) {
         int off = 0;
-        for (int s = 1; s < i; ++s) off += ((1 << logr(s)) - 1) << logp(s);
+        for (int s = 1; s < i; ++s) off += tw_count(s);
         return off;
     }
     __host__ __device__ static constexpr int tw_entries() { return tw_offset(NSUB); }
 };
 
+// a * W_16^I for a compile-time I (exact special cases where they exist).
+template <int I>
+__device__ __forceinline__ float2 mul_w16c(float2 a) {
+    constexpr int i = I & 15;
+    if constexpr (i == 0) return a;
+    else if constexpr (i == 1) return mul_w16_1(a);
+    else if constexpr (i == 2) return mul_w8_1(a);
+    else if constexpr (i == 3) return mul_w16_3(a);
+    else if constexpr (i == 4) return mul_mi(a);
+    else if constexpr (i == 6) return mul_w8_3(a);
+    else if constexpr (i == 8) return make_float2(-a.x, -a.y);
+    else if constexpr (i == 9) return mul_w16_9(a);
+    else if constexpr (i > 8) {
+        const float2 b = mul_w16c<i - 8>(a);
+        return make_float2(-b.x, -b.y);
+    } else {  // 5, 7
+        const float2 b = mul_w16c<i - 4>(a);
+        return mul_mi(b);
+    }
+}
+
+template <int LOGE, int LOGR, int B, int M>
+struct FactoredTw {
+    // W_E^{m b} with E = 2^LOGE expressed in sixteenths of a turn
+    static constexpr int idx16 = ((M * B) << (4 - LOGE)) & 15;
+};
+
 // Butterflies of one sub-pass on the register array v.
-template <int LOGE, int LOGR, int LOGP, int LOGT>
+template <int LOGE, int LOGR, int LOGP, int LOGT, bool FACT = false>
 __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, const float2 *tw) {
     constexpr int E = 1 << LOGE, R = 1 << LOGR, NB = E / R, P = 1 << LOGP, T = 1 << LOGT;
+    if constexpr (FACT) {
+        float2 wt[R];
 #pragma unroll
-    for (int b = 0; b < NB; ++b) {
-        float2 x[R];
+        for (int m = 1; m < R; ++m) wt[m] = ld_tw(tw + (m - 1) * T + t);
+        auto body = [&](auto bc) {
+            constexpr int b = decltype(bc)::value;
+            float2 x[R];
 #pragma unroll
-        for (int m = 0; m < R; ++m) x[m] = v[b + m * NB];
-        if (LOGP > 0) {
-            const int j = t + T * b;
-            const int k = j & (P - 1);
+            for (int m = 0; m < R; ++m) x[m] = v[b + m * NB];
+            [&]<int... Ms>(std::integer_sequence<int, Ms...>) {
+                ((Ms > 0 ? (x[Ms] = cmul(mul_w16c<FactoredTw<LOGE, LOGR, b, Ms>::idx16>(x[Ms]), wt[Ms]), 0) : 0), ...);
+            }(std::make_integer_sequence<int, R>{});
+            Dft<R>::run(x);
 #pragma unroll
-            for (int m = 1; m < R; ++m) x[m] = cmul(x[m], ld_tw(tw + (m - 1) * P + k));
+            for (int q = 0; q < R; ++q) v[b + q * NB] = x[q];
+        };
+        [&]<int... Bs>(std::integer_sequence<int, Bs...>) {
+            (body(std::integral_constant<int, Bs>{}), ...);
+        }(std::make_integer_sequence<int, NB>{});
+    } else {
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            float2 x[R];
+#pragma unroll
+            for (int m = 0; m < R; ++m) x[m] = v[b + m * NB];
+            if (LOGP > 0) {
+                const int j = t + T * b;
+                const int k = j & (P - 1);
+#pragma unroll
+                for (int m = 1; m < R; ++m) x[m] = cmul(x[m], ld_tw(tw + (m - 1) * P + k));
+            }
+            Dft<R>::run(x);
+#pragma unroll
+            for (int q = 0; q < R; ++q) v[b + q * NB] = x[q];
         }
-        Dft<R>::run(x);
-#pragma unroll
-        for (int q = 0; q < R; ++q) v[b + q * NB] = x[q];
     }
+}
+
+// Twiddle-table segments of sub-passes 1..NSUB-1 (offsets from `base`).
+template <int LOGN>
+inline int subcfg_segments(TwiddleSegment *out, uint64_t base) {
+    using C = SubCfg<LOGN>;
+    for (int i = 1; i < C::NSUB; ++i)
+        out[i - 1] = TwiddleSegment{base + (uint64_t)C::tw_offset(i), (uint64_t)C::tw_count(i), 0, C::tw_logm(i),
+                                    C::tw_logp(i), 0};
+    return C::NSUB - 1;
+}
+
+// Sub-pass I of the schedule of SubCfg<LOGN> (twiddle table already offset).
+template <int LOGN, int I>
+__device__ __forceinline__ void subpass_run(float2 (&v)[SubCfg<LOGN>::E], int t, const float2 *tw_all) {
+    using C = SubCfg<LOGN>;
+    subpass_compute<C::LOGE, C::logr(I), C::logp(I), C::LOGT, C::factored(I)>(v, t, tw_all + C::tw_offset(I));
 }
 
 // Position (within the transform) of output q of butterfly slot b after

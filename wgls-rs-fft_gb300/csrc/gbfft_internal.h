@@ -12,27 +12,11 @@ constexpr int kMaxLogN = 30;          // largest supported transform: 2^30 sampl
 constexpr int kRowsMaxLogN = 14;      // single-pass (in shared memory) limit
 constexpr int kMaxSub = 16;
 
-// ---- single-pass kernel (fft_rows.cu) ------------------------------------
-struct RowsKernelInfo {
-    const void *fn = nullptr;
-    int threads = 0;
-    int transforms_per_cta = 0;
-    size_t smem = 0;
-    int nsub = 0;
-    int sub_logr[kMaxSub] = {};
-    int sub_logp[kMaxSub] = {};
-    int tw_entries = 0;  // complex entries of the concatenated sub-pass tables
-};
-bool rows_kernel_info(int logn, RowsKernelInfo &k);
-cudaError_t rows_prepare(const RowsKernelInfo &k);
-cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
-                        const float2 *tw, int direction, int logn, cudaStream_t stream);
-
 // ---- twiddle generation (twiddle.cu) -------------------------------------
 // A segment fills `count` complex entries at `offset` of a table with
 // W_M^{e(i)} = exp(-2 pi i e(i) / M), M = 2^logm, computed in FP64 and
 // rounded to FP32.
-//   kind 0 (sub-pass table): i = (m-1)*P + k, e = m*k, P = 2^logp, M = R*P
+//   kind 0 (sub-pass table): i = (m-1)*P + k, e = m*k, P = 2^logp
 //   kind 1 (linear table):   e = i << logstride
 struct TwiddleSegment {
     uint64_t offset;
@@ -43,5 +27,20 @@ struct TwiddleSegment {
     int logstride;
 };
 cudaError_t twiddle_fill(float2 *table, const TwiddleSegment *segs, int nseg, cudaStream_t stream);
+
+// ---- single-pass kernel (fft_rows.cu) ------------------------------------
+struct RowsKernelInfo {
+    const void *fn = nullptr;
+    int threads = 0;
+    int transforms_per_cta = 0;
+    size_t smem = 0;
+    TwiddleSegment segs[kMaxSub] = {};  // sub-pass tables, offsets from 0
+    int nseg = 0;
+    int tw_entries = 0;
+};
+bool rows_kernel_info(int logn, RowsKernelInfo &k);
+cudaError_t rows_prepare(const RowsKernelInfo &k);
+cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
+                        const float2 *tw, int direction, int logn, cudaStream_t stream);
 
 }  // namespace gbfft

@@ -76,29 +76,19 @@ int na_setup(int dev, cudaStream_t stream, NaDevice &d) {
     for (int L = kNaMinLogN; L <= kNaMaxLogN; ++L) {
         std::vector<int> parts = split_passes(L);
         if (parts.size() != 2) return GBFFT_ERR_UNSUPPORTED;
-        std::vector<TwiddleSegment> segs;
-        NaPlan &np = d.plan[L];
+        std::vector<PassDesc> passes(2);
         int logp = 0;
         for (int i = 0; i < 2; ++i) {
-            std::vector<int> lr, lp;
-            if (!pass_kernel_info(parts[i], i == 0, np.pass[i], lr, lp)) return GBFFT_ERR_UNSUPPORTED;
-            if (pass_prepare(np.pass[i]) != cudaSuccess) return GBFFT_ERR_CUDA;
-            np.pass[i].logp = logp;
-            np.pass[i].sub_tw_offset = off;
-            for (size_t s = 1; s < lr.size(); ++s) {
-                TwiddleSegment seg = {off, (uint64_t)((1 << lr[s]) - 1) << lp[s], 0, lr[s] + lp[s], lp[s], 0};
-                segs.push_back(seg);
-                off += seg.count;
-            }
+            if (!pass_kernel_info(parts[i], i == 0, passes[i])) return GBFFT_ERR_UNSUPPORTED;
+            if (pass_prepare(passes[i]) != cudaSuccess) return GBFFT_ERR_CUDA;
+            passes[i].logp = logp;
             logp += parts[i];
         }
-        np.split = (L + 1) / 2;
-        np.lo_off = off;
-        segs.push_back({off, 1ull << np.split, 1, L, 0, 0});
-        off += 1ull << np.split;
-        np.hi_off = off;
-        segs.push_back({off, 1ull << (L - np.split), 1, L, 0, np.split});
-        off += 1ull << (L - np.split);
+        std::vector<TwiddleSegment> segs;
+        NaPlan &np = d.plan[L];
+        off = multipass_segments(L, passes, off, segs, np.lo_off, np.hi_off, np.split);
+        np.pass[0] = passes[0];
+        np.pass[1] = passes[1];
         if (off > kNaTwiddleEntries) return GBFFT_ERR_UNSUPPORTED;
         if (twiddle_fill(d.tw, segs.data(), (int)segs.size(), stream) != cudaSuccess) return GBFFT_ERR_CUDA;
     }

@@ -39,26 +39,25 @@ std::vector<int> split_passes(int logn) {
     return parts;
 }
 
-static void add_sub_segments(std::vector<TwiddleSegment> &segs, uint64_t base, const std::vector<int> &logr,
-                             const std::vector<int> &logp) {
-    uint64_t off = base;
-    for (size_t i = 1; i < logr.size(); ++i) {
-        TwiddleSegment s;
-        s.offset = off;
-        s.count = (uint64_t)((1 << logr[i]) - 1) << logp[i];
-        s.kind = 0;
-        s.logm = logr[i] + logp[i];
-        s.logp = logp[i];
-        s.logstride = 0;
-        segs.push_back(s);
-        off += s.count;
+uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t off,
+                            std::vector<TwiddleSegment> &segs, uint64_t &lo_off, uint64_t &hi_off, int &split) {
+    for (PassDesc &d : passes) {
+        d.sub_tw_offset = off;
+        for (int s = 0; s < d.nseg; ++s) {
+            TwiddleSegment seg = d.segs[s];
+            seg.offset += off;
+            segs.push_back(seg);
+        }
+        off += (uint64_t)d.tw_entries;
     }
-}
-
-static uint64_t sub_entries(const std::vector<int> &logr, const std::vector<int> &logp) {
-    uint64_t n = 0;
-    for (size_t i = 1; i < logr.size(); ++i) n += (uint64_t)((1 << logr[i]) - 1) << logp[i];
-    return n;
+    split = (logn + 1) / 2;
+    lo_off = off;
+    segs.push_back(TwiddleSegment{off, 1ull << split, 1, logn, 0, 0});
+    off += 1ull << split;
+    hi_off = off;
+    segs.push_back(TwiddleSegment{off, 1ull << (logn - split), 1, logn, 0, split});
+    off += 1ull << (logn - split);
+    return off;
 }
 
 int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
@@ -74,20 +73,16 @@ int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;
         }
-        std::vector<int> lr(p.rows.sub_logr, p.rows.sub_logr + p.rows.nsub);
-        std::vector<int> lp(p.rows.sub_logp, p.rows.sub_logp + p.rows.nsub);
-        add_sub_segments(segs, 0, lr, lp);
+        segs.assign(p.rows.segs, p.rows.segs + p.rows.nseg);
         p.tw_entries = p.rows.tw_entries;
     } else {
         p.multipass = true;
         p.needs_workspace = true;
         std::vector<int> parts = split_passes(logn);
-        uint64_t off = 0;
         int logp = 0;
         for (size_t i = 0; i < parts.size(); ++i) {
             PassDesc d;
-            std::vector<int> lr, lp;
-            if (!pass_kernel_info(parts[i], i == 0, d, lr, lp)) {
+            if (!pass_kernel_info(parts[i], i == 0, d)) {
                 why = "no pass kernel for radix 2^" + std::to_string(parts[i]);
                 return GBFFT_ERR_UNSUPPORTED;
             }
@@ -96,22 +91,10 @@ int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
                 return GBFFT_ERR_CUDA;
             }
             d.logp = logp;
-            d.sub_tw_offset = off;
-            add_sub_segments(segs, off, lr, lp);
-            off += sub_entries(lr, lp);
             logp += parts[i];
             p.passes.push_back(d);
         }
-        p.tw_split = (logn + 1) / 2;
-        p.tw_lo_offset = off;
-        TwiddleSegment lo = {off, 1ull << p.tw_split, 1, logn, 0, 0};
-        off += lo.count;
-        p.tw_hi_offset = off;
-        TwiddleSegment hi = {off, 1ull << (logn - p.tw_split), 1, logn, 0, p.tw_split};
-        off += hi.count;
-        segs.push_back(lo);
-        segs.push_back(hi);
-        p.tw_entries = off;
+        p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
     }
     if (p.tw_entries > 0) {
         if ((e = cudaMalloc(&p.tw, p.tw_entries * sizeof(float2))) != cudaSuccess) {

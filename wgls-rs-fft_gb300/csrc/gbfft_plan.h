@@ -27,7 +27,10 @@ struct PassDesc {
     int cols = 0;        // columns (independent length-R DFTs) per CTA
     int threads = 0;
     size_t smem = 0;
-    uint64_t sub_tw_offset = 0;  // this pass's in-SMEM sub-pass tables
+    uint64_t sub_tw_offset = 0;         // where this pass's sub-pass tables start
+    TwiddleSegment segs[kMaxSub] = {};  // its in-SMEM sub-pass tables, offsets from 0
+    int nseg = 0;
+    int tw_entries = 0;
 };
 
 struct Plan {
@@ -46,7 +49,7 @@ struct Plan {
 };
 
 // fft_passes.cu
-bool pass_kernel_info(int logr, bool first, PassDesc &d, std::vector<int> &sub_logr, std::vector<int> &sub_logp);
+bool pass_kernel_info(int logr, bool first, PassDesc &d);
 cudaError_t pass_prepare(const PassDesc &d);
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
@@ -54,6 +57,13 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
 
 // log2 radices of the global passes for a multi-pass transform of 2^logn.
 std::vector<int> split_passes(int logn);
+
+// Append the twiddle segments of a multi-pass schedule (per-pass sub-pass
+// tables, then the two-level W_N table) starting at `offset`; fills the pass
+// descriptors' table offsets and the plan-level two-level table fields.
+// Returns the offset one past the last entry.
+uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t offset,
+                            std::vector<TwiddleSegment> &segs, uint64_t &lo_off, uint64_t &hi_off, int &split);
 
 int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why);
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(LIB_DIR, "libgbfft.so")
 INCLUDE = os.path.join(REPO_ROOT, "include")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
+NVCC_FLAGS = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
               "--expt-relaxed-constexpr"]
 
 

@@ -116,6 +116,56 @@ int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,
 int gbfft_c2c_device_noalloc(const void *d_in, void *d_out, uint64_t n,
                              uint64_t batch, int direction, void *stream);
 
+/* ---- ragged batches (no reference counterpart: the reference rejects rows
+ * of different lengths, src/lib.rs:526-533, so mixed sizes cost one call per
+ * size there) ---------------------------------------------------------------
+ * Transforms of mixed power-of-two lengths (2^0 .. 2^18) and directions,
+ * packed anywhere in one device buffer, run in ONE persistent kernel launch
+ * fed by a device work queue.  Descriptor i transforms the 2^log2n complex
+ * samples starting `offset` samples into d_in and writes them at the same
+ * offset in d_out.  Transforms must not overlap each other; d_in may equal
+ * d_out. */
+typedef struct gbfft_ragged_desc {
+    uint64_t offset;   /* in complex samples */
+    uint32_t log2n;    /* 0 .. 18 */
+    int32_t direction; /* GBFFT_FORWARD or GBFFT_INVERSE */
+} gbfft_ragged_desc;
+
+typedef struct gbfft_ragged_plan gbfft_ragged_plan;
+
+/* Options for gbfft_ragged_plan_set. */
+#define GBFFT_RAGGED_OPT_SPIN_LIMIT 1          /* polls before a dependency wait gives up */
+#define GBFFT_RAGGED_OPT_TEST_DROP_PRODUCERS 2 /* test hook: omit first-pass items */
+
+/* Build the work queue, twiddle tables and workspace for a descriptor set
+ * (validated here; errors are reported on `ctx`). */
+int gbfft_ragged_plan_create(gbfft_ctx *ctx, const gbfft_ragged_desc *descs, uint32_t count,
+                             gbfft_ragged_plan **out_plan);
+
+int gbfft_ragged_plan_set(gbfft_ragged_plan *plan, int option, uint64_t value);
+
+/* Enqueue the plan on `stream` (NULL = default stream).  `capacity` is the
+ * size of d_in and of d_out in complex samples; a descriptor reaching past it
+ * is rejected (GBFFT_ERR_INVALID_ARGUMENT) before anything is launched.  With
+ * use_graph != 0 the reset + launch sequence is captured once into a CUDA
+ * graph (per (d_in, d_out) pair) and replayed.  Asynchronous: call
+ * gbfft_ragged_wait. */
+int gbfft_ragged_execute(gbfft_ragged_plan *plan, const void *d_in, void *d_out, uint64_t capacity,
+                         int use_graph, void *stream);
+
+/* Synchronise `stream` and report GBFFT_ERR_TIMEOUT if a dependency wait of
+ * the last execution gave up. */
+int gbfft_ragged_wait(gbfft_ragged_plan *plan, void *stream);
+
+/* Number of kernel launches issued by the plan so far. */
+uint64_t gbfft_ragged_launch_count(const gbfft_ragged_plan *plan);
+
+void gbfft_ragged_plan_destroy(gbfft_ragged_plan *plan);
+
+/* One-shot: create, execute (no graph), wait, destroy. */
+int gbfft_ragged_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t capacity,
+                        const gbfft_ragged_desc *descs, uint32_t count, void *stream);
+
 /* Replaces GpuFftTrait::benchmark_gpu_only (src/lib.rs:108-156, 673-707):
  * device-only timing of `iters` transforms of an n x batch device batch after
  * `warmup` untimed ones, with CUDA events on the context's stream.  Writes the

@@ -1,0 +1,561 @@
+// Ragged batches: transforms of mixed power-of-two sizes (2^0 .. 2^18) and
+// directions, packed back to back, in ONE persistent launch fed by a device
+// work queue.  The reference has no such mode -- its GpuFft requires every row
+// of a batch to have the same length (larsjoost/wgls-rs-fft src/lib.rs:526-533)
+// -- so a ragged workload there is one call per size.
+//
+// Work items (all move 8192 samples through HBM once):
+//   kind 0  G = 8192/N whole transforms of one size N <= 2^13 (single pass)
+//   kind 1  first global pass of a transform of N = 2^14 .. 2^18, 16*NG columns
+//   kind 2  second global pass of such a transform, 16*NG columns
+// Items are queued kind 1, then kind 0, then kind 2, and every CTA takes the
+// next item with one atomicAdd.  A kind-2 item depends on all kind-1 items of
+// its transform, which all sit earlier in the queue and are therefore already
+// owned by running CTAs that never wait: the wait always ends.  Each wait is
+// still bounded (spin_limit polls with __nanosleep): on expiry the kernel sets
+// an error flag, every CTA stops taking items, and the host reports
+// GBFFT_ERR_TIMEOUT.
+//
+// First-pass output goes to a workspace; producers publish with
+// __threadfence + atomicAdd, the consumer polls with ld.acquire.gpu and reads
+// the workspace with L1-bypassing loads.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gbfft_internal.h"
+#include "gbfft_plan.h"
+#include "gbfft_ragged.h"
+#include "fft_tiles.cuh"
+
+namespace gbfft {
+
+constexpr int kRagThreads = 512;
+constexpr int kRagMaxLogN = 18;
+constexpr int kRagRowsMaxLogN = 13;
+
+struct RagXform {
+    uint64_t offset;     // complex samples from the start of in/out
+    uint64_t ws_offset;  // two-pass transforms: start of their workspace slice
+    int32_t logn;
+    int32_t dir;         // GBFFT_FORWARD / GBFFT_INVERSE
+    uint32_t tiles1;     // two-pass transforms: number of first-pass items
+    uint32_t pad;
+};
+
+struct RagItem {
+    uint32_t kind;
+    uint32_t a;  // kind 0: first index into order[]; kind 1/2: transform id
+    uint32_t b;  // kind 0: transforms in the item;   kind 1/2: tile index
+    uint32_t logn;
+};
+
+struct RagParams {
+    const float2 *in;
+    float2 *out;
+    float2 *ws;
+    const RagItem *items;
+    uint32_t nitems;
+    uint32_t spin_limit;
+    const RagXform *xf;
+    const uint32_t *order;
+    uint32_t *item_counter;
+    uint32_t *done1;
+    uint32_t *error;
+    const float2 *sub[16];   // sub-pass tables of a length-2^L in-SMEM FFT
+    const float2 *lo[kRagMaxLogN + 1];
+    const float2 *hi[kRagMaxLogN + 1];
+    int split[kRagMaxLogN + 1];
+};
+
+__host__ __device__ constexpr int rag_logr1(int L) { return L / 2 + (L & 1); }
+__host__ __device__ constexpr int rag_logr2(int L) { return L / 2; }
+__host__ __device__ constexpr int rag_groups(int logr) { return kRagThreads / (kCols << (logr - 4)); }
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <int L>
+__device__ __forceinline__ void rag_rows(const RagParams &P, const RagItem &it, float2 *smem) {
+    constexpr int G = kRagThreads / SubCfg<L>::T;
+    auto ref = [&](int g) {
+        const bool act = (uint32_t)g < it.b;
+        const RagXform x = P.xf[P.order[it.a + (act ? g : 0)]];
+        const bool inv = x.dir == GBFFT_INVERSE;
+        const float sc = inv ? ldexpf(1.0f, -L) : 1.0f;
+        return RowRef{P.in + x.offset, P.out + x.offset, act, inv ? -1.0f : 1.0f, sc, inv ? -sc : 1.0f};
+    };
+    rows_tile<L, G>(ref, P.sub[L], smem);
+}
+
+// Returns false when the wait for the first pass gave up.
+template <int LOGR, bool FIRST>
+__device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, float2 *smem) {
+    constexpr int NG = rag_groups(LOGR);
+    __shared__ int s_abort;
+    const RagXform x = P.xf[it.a];
+    const int L = x.logn;
+    if (!FIRST) {
+        if (threadIdx.x == 0) {
+            uint32_t polls = 0;
+            int abort = 0;
+            while (ld_acquire_gpu(P.done1 + it.a) < x.tiles1) {
+                if (++polls > P.spin_limit) {
+                    atomicExch(P.error, 1u);
+                    abort = 1;
+                    break;
+                }
+                __nanosleep(256);
+            }
+            s_abort = abort;
+        }
+        __syncthreads();
+        if (s_abort) return false;
+    }
+    const bool inv = x.dir == GBFFT_INVERSE;
+    const float sc = inv ? ldexpf(1.0f, -L) : 1.0f;
+    PassArgs a;
+    a.src = FIRST ? P.in + x.offset : P.ws + x.ws_offset;
+    a.dst = FIRST ? P.ws + x.ws_offset : P.out + x.offset;
+    a.logn = L;
+    a.logp = FIRST ? 0 : rag_logr1(L);
+    a.col0 = it.b * (uint32_t)(kCols * NG);
+    a.tw_sub = P.sub[LOGR];
+    a.tw_lo = P.lo[L];
+    a.tw_hi = P.hi[L];
+    a.tw_split = P.split[L];
+    a.in_im = (FIRST && inv) ? -1.0f : 1.0f;
+    a.out_re = FIRST ? 1.0f : sc;
+    a.out_im = FIRST ? 1.0f : (inv ? -sc : 1.0f);
+    a.coherent_load = !FIRST;
+    pass_tile<LOGR, NG, FIRST>(a, smem);
+    if (FIRST) {
+        __threadfence();  // this thread's workspace stores are visible GPU-wide
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(P.done1 + it.a, 1u);
+    }
+    return true;
+}
+
+template <bool FIRST>
+__device__ __forceinline__ bool rag_pass_dispatch(const RagParams &P, const RagItem &it, float2 *smem) {
+    const int logr = FIRST ? rag_logr1(it.logn) : rag_logr2(it.logn);
+    switch (logr) {
+        case 7: return rag_pass<7, FIRST>(P, it, smem);
+        case 8: return rag_pass<8, FIRST>(P, it, smem);
+        case 9: return rag_pass<9, FIRST>(P, it, smem);
+        default: return true;
+    }
+}
+
+__global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P) {
+    extern __shared__ float2 smem_rag[];
+    __shared__ uint32_t s_item;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const bool stop = *(volatile uint32_t *)P.error != 0u;
+            s_item = stop ? 0xffffffffu : atomicAdd(P.item_counter, 1u);
+        }
+        __syncthreads();
+        const uint32_t idx = s_item;
+        if (idx >= P.nitems) break;
+        const RagItem it = P.items[idx];
+        bool ok = true;
+        if (it.kind == 0) {
+            switch (it.logn) {
+#define GBFFT_RAG_ROWS(L) \
+    case L: rag_rows<L>(P, it, smem_rag); break;
+                GBFFT_RAG_ROWS(0) GBFFT_RAG_ROWS(1) GBFFT_RAG_ROWS(2) GBFFT_RAG_ROWS(3) GBFFT_RAG_ROWS(4)
+                GBFFT_RAG_ROWS(5) GBFFT_RAG_ROWS(6) GBFFT_RAG_ROWS(7) GBFFT_RAG_ROWS(8) GBFFT_RAG_ROWS(9)
+                GBFFT_RAG_ROWS(10) GBFFT_RAG_ROWS(11) GBFFT_RAG_ROWS(12) GBFFT_RAG_ROWS(13)
+#undef GBFFT_RAG_ROWS
+                default: break;
+            }
+        } else if (it.kind == 1) {
+            ok = rag_pass_dispatch<true>(P, it, smem_rag);
+        } else {
+            ok = rag_pass_dispatch<false>(P, it, smem_rag);
+        }
+        if (!ok) break;
+        __syncthreads();  // shared memory and s_item are reused by the next item
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static size_t rag_smem_bytes() {
+    size_t m = (size_t)kRagThreads * 16 * sizeof(float2);  // rows items
+    for (int lr = 7; lr <= 9; ++lr) {
+        const int ng = rag_groups(lr);
+        m = std::max(m, ((size_t)ng * kCols * (1u << lr) + (size_t)ng * kCols * 17) * sizeof(float2));
+    }
+    return m;
+}
+
+template <int L>
+static int rag_sub_segments(TwiddleSegment *out, uint64_t base) { return subcfg_segments<L>(out, base); }
+
+static int sub_segments(int L, TwiddleSegment *out, uint64_t base, int &entries) {
+    switch (L) {
+#define GBFFT_RAG_SEG(X) \
+    case X: entries = SubCfg<X>::tw_entries(); return rag_sub_segments<X>(out, base);
+        GBFFT_RAG_SEG(0) GBFFT_RAG_SEG(1) GBFFT_RAG_SEG(2) GBFFT_RAG_SEG(3) GBFFT_RAG_SEG(4) GBFFT_RAG_SEG(5)
+        GBFFT_RAG_SEG(6) GBFFT_RAG_SEG(7) GBFFT_RAG_SEG(8) GBFFT_RAG_SEG(9) GBFFT_RAG_SEG(10)
+        GBFFT_RAG_SEG(11) GBFFT_RAG_SEG(12) GBFFT_RAG_SEG(13)
+#undef GBFFT_RAG_SEG
+        default: entries = 0; return 0;
+    }
+}
+
+struct RaggedPlanImpl {
+    int device = 0;
+    uint32_t count = 0;
+    uint32_t nitems = 0;
+    uint64_t ws_samples = 0;
+    uint64_t total_samples = 0;
+    uint64_t max_extent = 0;  // one past the last sample any transform touches
+    uint32_t spin_limit = 1u << 22;
+    bool drop_producers = false;
+    bool dirty = true;        // items must be (re)uploaded
+    std::vector<RagXform> xf;
+    std::vector<RagItem> items;
+    std::vector<uint32_t> order;
+    std::vector<TwiddleSegment> segs;
+    uint64_t tw_entries = 0;
+    uint64_t sub_off[16] = {};
+    uint64_t lo_off[kRagMaxLogN + 1] = {}, hi_off[kRagMaxLogN + 1] = {};
+    int split[kRagMaxLogN + 1] = {};
+    bool need_sub[16] = {}, need_2l[kRagMaxLogN + 1] = {};
+    DeviceBuffer meta;        // xf | items | order | counters
+    DeviceBuffer tw;
+    DeviceBuffer ws;
+    uint32_t *h_error = nullptr;  // pinned copy of the error flag
+    size_t off_items = 0, off_order = 0, off_counters = 0, counters_bytes = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    const void *g_in = nullptr;
+    void *g_out = nullptr;
+    cudaStream_t capture_stream = nullptr;
+    uint64_t launches = 0;
+    int sms = 0;
+};
+
+static void build_items(RaggedPlanImpl &p) {
+    p.items.clear();
+    p.order.clear();
+    std::vector<std::vector<uint32_t>> by_size(kRagRowsMaxLogN + 1);
+    // kind 1 first
+    for (uint32_t i = 0; i < p.count; ++i) {
+        const RagXform &x = p.xf[i];
+        if (x.logn > kRagRowsMaxLogN) {
+            if (p.drop_producers) continue;  // test hook: nothing will publish the first pass
+            for (uint32_t t = 0; t < x.tiles1; ++t) p.items.push_back(RagItem{1, i, t, (uint32_t)x.logn});
+        } else {
+            by_size[x.logn].push_back(i);
+        }
+    }
+    // kind 0, largest sizes first
+    for (int L = kRagRowsMaxLogN; L >= 0; --L) {
+        const uint32_t g = (uint32_t)(kRagThreads / (1 << (L < 4 ? 0 : L - 4)));
+        const std::vector<uint32_t> &ids = by_size[L];
+        for (size_t s = 0; s < ids.size(); s += g) {
+            const uint32_t first = (uint32_t)p.order.size();
+            const uint32_t n = (uint32_t)std::min<size_t>(g, ids.size() - s);
+            for (uint32_t k = 0; k < n; ++k) p.order.push_back(ids[s + k]);
+            p.items.push_back(RagItem{0, first, n, (uint32_t)L});
+        }
+    }
+    // kind 2 last
+    for (uint32_t i = 0; i < p.count; ++i) {
+        const RagXform &x = p.xf[i];
+        if (x.logn > kRagRowsMaxLogN) {
+            const int lr2 = rag_logr2(x.logn);
+            const uint32_t tiles2 = (1u << (x.logn - lr2)) / (uint32_t)(kCols * rag_groups(lr2));
+            for (uint32_t t = 0; t < tiles2; ++t) p.items.push_back(RagItem{2, i, t, (uint32_t)x.logn});
+        }
+    }
+    if (p.order.empty()) p.order.push_back(0);
+    p.nitems = (uint32_t)p.items.size();
+    p.dirty = true;
+}
+
+int ragged_plan_build(RaggedPlanImpl *&out, int device, const gbfft_ragged_desc *descs, uint32_t count,
+                      std::string &why) {
+    out = nullptr;
+    RaggedPlanImpl *p = new RaggedPlanImpl();
+    p->device = device;
+    p->count = count;
+    p->xf.resize(count);
+    uint64_t ws = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        const gbfft_ragged_desc &d = descs[i];
+        if (d.log2n > kRagMaxLogN) {
+            why = "ragged transforms are limited to N <= 2^18 (descriptor " + std::to_string(i) + ")";
+            delete p;
+            return GBFFT_ERR_UNSUPPORTED;
+        }
+        if (d.direction != GBFFT_FORWARD && d.direction != GBFFT_INVERSE) {
+            why = "descriptor " + std::to_string(i) + ": direction must be -1 or +1";
+            delete p;
+            return GBFFT_ERR_INVALID_ARGUMENT;
+        }
+        RagXform &x = p->xf[i];
+        x.offset = d.offset;
+        x.logn = (int32_t)d.log2n;
+        x.dir = d.direction;
+        x.ws_offset = 0;
+        x.tiles1 = 0;
+        x.pad = 0;
+        const uint64_t n = 1ull << d.log2n;
+        p->total_samples += n;
+        p->max_extent = std::max(p->max_extent, d.offset + n);
+        if ((int)d.log2n > kRagRowsMaxLogN) {
+            const int lr1 = rag_logr1(d.log2n);
+            x.ws_offset = ws;
+            ws += n;
+            x.tiles1 = (uint32_t)((1ull << (d.log2n - lr1)) / (uint64_t)(kCols * rag_groups(lr1)));
+            p->need_sub[lr1] = p->need_sub[rag_logr2(d.log2n)] = true;
+            p->need_2l[d.log2n] = true;
+        } else {
+            p->need_sub[d.log2n] = true;
+        }
+    }
+    p->ws_samples = ws;
+    // twiddle tables
+    uint64_t off = 0;
+    for (int L = 0; L < 16; ++L) {
+        if (!p->need_sub[L]) continue;
+        TwiddleSegment tmp[kMaxSub];
+        int entries = 0;
+        const int ns = sub_segments(L, tmp, off, entries);
+        p->sub_off[L] = off;
+        for (int s = 0; s < ns; ++s) p->segs.push_back(tmp[s]);
+        off += (uint64_t)entries;
+    }
+    for (int L = kRagRowsMaxLogN + 1; L <= kRagMaxLogN; ++L) {
+        if (!p->need_2l[L]) continue;
+        const int s = (L + 1) / 2;
+        p->split[L] = s;
+        p->lo_off[L] = off;
+        p->segs.push_back(TwiddleSegment{off, 1ull << s, 1, L, 0, 0});
+        off += 1ull << s;
+        p->hi_off[L] = off;
+        p->segs.push_back(TwiddleSegment{off, 1ull << (L - s), 1, L, 0, s});
+        off += 1ull << (L - s);
+    }
+    p->tw_entries = off;
+    build_items(*p);
+    out = p;
+    return GBFFT_OK;
+}
+
+int ragged_plan_upload(RaggedPlanImpl &p, cudaStream_t stream, std::string &why) {
+    if (p.sms == 0) {
+        cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, p.device);
+        cudaError_t e = cudaFuncSetAttribute((const void *)fft_ragged_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rag_smem_bytes());
+        if (e != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+    }
+    if (!p.h_error) {
+        if (cudaHostAlloc(&p.h_error, sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            why = "pinned error flag";
+            return GBFFT_ERR_OUT_OF_MEMORY;
+        }
+        *p.h_error = 0;
+    }
+    if (p.tw.ptr == nullptr && p.tw_entries > 0) {
+        int st = p.tw.ensure(p.tw_entries * sizeof(float2), why);
+        if (st != GBFFT_OK) return st;
+        for (size_t s = 0; s < p.segs.size(); s += 16) {
+            const int n = (int)std::min<size_t>(16, p.segs.size() - s);
+            cudaError_t e = twiddle_fill((float2 *)p.tw.ptr, p.segs.data() + s, n, stream);
+            if (e != cudaSuccess) {
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_CUDA;
+            }
+        }
+    }
+    if (p.ws_samples > 0) {
+        int st = p.ws.ensure(p.ws_samples * sizeof(float2), why);
+        if (st != GBFFT_OK) return st;
+    }
+    if (!p.dirty) return GBFFT_OK;
+    const size_t xf_bytes = p.xf.size() * sizeof(RagXform);
+    const size_t it_bytes = p.items.size() * sizeof(RagItem);
+    const size_t or_bytes = p.order.size() * sizeof(uint32_t);
+    p.off_items = (xf_bytes + 255) & ~(size_t)255;
+    p.off_order = (p.off_items + it_bytes + 255) & ~(size_t)255;
+    p.off_counters = (p.off_order + or_bytes + 255) & ~(size_t)255;
+    p.counters_bytes = (2 + (size_t)p.count) * sizeof(uint32_t);
+    int st = p.meta.ensure(p.off_counters + p.counters_bytes, why);
+    if (st != GBFFT_OK) return st;
+    std::vector<char> host(p.off_counters, 0);
+    if (xf_bytes) memcpy(host.data(), p.xf.data(), xf_bytes);
+    if (it_bytes) memcpy(host.data() + p.off_items, p.items.data(), it_bytes);
+    memcpy(host.data() + p.off_order, p.order.data(), or_bytes);
+    cudaError_t e = cudaMemcpyAsync(p.meta.ptr, host.data(), host.size(), cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        why = cudaGetErrorString(e);
+        return GBFFT_ERR_CUDA;
+    }
+    p.dirty = false;
+    return GBFFT_OK;
+}
+
+static RagParams rag_params(const RaggedPlanImpl &p, const void *in, void *out) {
+    RagParams P;
+    memset(&P, 0, sizeof P);
+    char *m = (char *)p.meta.ptr;
+    P.in = (const float2 *)in;
+    P.out = (float2 *)out;
+    P.ws = (float2 *)p.ws.ptr;
+    P.items = (const RagItem *)(m + p.off_items);
+    P.nitems = p.nitems;
+    P.spin_limit = p.spin_limit;
+    P.xf = (const RagXform *)m;
+    P.order = (const uint32_t *)(m + p.off_order);
+    uint32_t *ctr = (uint32_t *)(m + p.off_counters);
+    P.item_counter = ctr;
+    P.error = ctr + 1;
+    P.done1 = ctr + 2;
+    const float2 *tw = (const float2 *)p.tw.ptr;
+    for (int L = 0; L < 16; ++L) P.sub[L] = p.need_sub[L] ? tw + p.sub_off[L] : nullptr;
+    for (int L = 0; L <= kRagMaxLogN; ++L) {
+        P.lo[L] = p.need_2l[L] ? tw + p.lo_off[L] : nullptr;
+        P.hi[L] = p.need_2l[L] ? tw + p.hi_off[L] : nullptr;
+        P.split[L] = p.split[L];
+    }
+    return P;
+}
+
+// Enqueue counters reset + persistent launch + error-flag readback on `s`.
+static cudaError_t rag_enqueue(RaggedPlanImpl &p, const void *in, void *out, cudaStream_t s) {
+    char *m = (char *)p.meta.ptr;
+    cudaError_t e = cudaMemsetAsync(m + p.off_counters, 0, p.counters_bytes, s);
+    if (e != cudaSuccess) return e;
+    RagParams P = rag_params(p, in, out);
+    if (p.nitems > 0) {
+        const unsigned grid = (unsigned)std::max(1, std::min<int>(2 * p.sms, (int)p.nitems));
+        void *args[] = {(void *)&P};
+        e = cudaLaunchKernel((const void *)fft_ragged_kernel, dim3(grid), dim3(kRagThreads), args, rag_smem_bytes(), s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaMemcpyAsync(p.h_error, m + p.off_counters + sizeof(uint32_t), sizeof(uint32_t),
+                           cudaMemcpyDeviceToHost, s);
+}
+
+int ragged_plan_execute(RaggedPlanImpl &p, const void *in, void *out, cudaStream_t stream, bool use_graph,
+                        std::string &why) {
+    int st = ragged_plan_upload(p, stream, why);
+    if (st != GBFFT_OK) return st;
+    cudaError_t e;
+    if (!use_graph) {
+        e = rag_enqueue(p, in, out, stream);
+        if (e != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        p.launches += p.nitems > 0 ? 1 : 0;
+        return GBFFT_OK;
+    }
+    if (p.graph_exec && (p.g_in != in || p.g_out != out)) {
+        cudaGraphExecDestroy(p.graph_exec);
+        cudaGraphDestroy(p.graph);
+        p.graph_exec = nullptr;
+        p.graph = nullptr;
+    }
+    if (!p.graph_exec) {
+        if (!p.capture_stream &&
+            cudaStreamCreateWithFlags(&p.capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+            why = "capture stream";
+            return GBFFT_ERR_CUDA;
+        }
+        e = cudaStreamBeginCapture(p.capture_stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e2 = rag_enqueue(p, in, out, p.capture_stream);
+            e = cudaStreamEndCapture(p.capture_stream, &p.graph);
+            if (e2 != cudaSuccess) e = e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p.graph_exec, p.graph, 0);
+        if (e != cudaSuccess) {
+            why = std::string("graph capture: ") + cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        p.g_in = in;
+        p.g_out = out;
+    }
+    e = cudaGraphLaunch(p.graph_exec, stream);
+    if (e != cudaSuccess) {
+        why = cudaGetErrorString(e);
+        return GBFFT_ERR_CUDA;
+    }
+    p.launches += p.nitems > 0 ? 1 : 0;
+    return GBFFT_OK;
+}
+
+int ragged_plan_wait(RaggedPlanImpl &p, cudaStream_t stream, std::string &why) {
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) {
+        why = cudaGetErrorString(e);
+        return GBFFT_ERR_CUDA;
+    }
+    if (p.h_error && *p.h_error) {
+        why = "a ragged second-pass item gave up waiting for its first pass";
+        *p.h_error = 0;
+        return GBFFT_ERR_TIMEOUT;
+    }
+    return GBFFT_OK;
+}
+
+int ragged_plan_set(RaggedPlanImpl &p, int option, uint64_t value, std::string &why) {
+    switch (option) {
+        case GBFFT_RAGGED_OPT_SPIN_LIMIT:
+            if (value == 0 || value > 0xffffffffull) {
+                why = "spin limit must be in [1, 2^32)";
+                return GBFFT_ERR_INVALID_ARGUMENT;
+            }
+            p.spin_limit = (uint32_t)value;
+            break;
+        case GBFFT_RAGGED_OPT_TEST_DROP_PRODUCERS:
+            p.drop_producers = value != 0;
+            build_items(p);
+            break;
+        default:
+            why = "unknown ragged plan option";
+            return GBFFT_ERR_INVALID_ARGUMENT;
+    }
+    if (p.graph_exec) {
+        cudaGraphExecDestroy(p.graph_exec);
+        cudaGraphDestroy(p.graph);
+        p.graph_exec = nullptr;
+        p.graph = nullptr;
+    }
+    return GBFFT_OK;
+}
+
+void ragged_plan_free(RaggedPlanImpl *p) {
+    if (!p) return;
+    if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->capture_stream) cudaStreamDestroy(p->capture_stream);
+    if (p->h_error) cudaFreeHost(p->h_error);
+    delete p;
+}
+
+uint64_t ragged_plan_samples(const RaggedPlanImpl &p) { return p.total_samples; }
+uint64_t ragged_plan_extent(const RaggedPlanImpl &p) { return p.max_extent; }
+uint32_t ragged_plan_items(const RaggedPlanImpl &p) { return p.nitems; }
+uint64_t ragged_plan_launches(const RaggedPlanImpl &p) { return p.launches; }
+
+}  // namespace gbfft

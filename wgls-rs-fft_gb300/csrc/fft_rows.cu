@@ -17,7 +17,7 @@
 // (a ^ ((a >> 4) * p & 15)); with that every exchange is free of bank
 // conflicts for N >= 256.
 #include "gbfft_internal.h"
-#include "fft_smem.cuh"
+#include "fft_tiles.cuh"
 
 namespace gbfft {
 
@@ -32,71 +32,17 @@ struct RowsCfg : SubCfg<LOGN> {
     static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * S::N * sizeof(float2) : 0;
 };
 
-__device__ __forceinline__ int swz(int a, int logp) {
-    return logp < 4 ? (a ^ (((a >> 4) << logp) & 15)) : a;
-}
-
-template <int LOGN, int I, bool DONE = (I >= SubCfg<LOGN>::NSUB)>
-struct RowsChain {
-    using C = SubCfg<LOGN>;
-    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, float2 *buf, const float2 *tw) {
-        constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);  // previous sub-pass
-        if (I > 1) __syncthreads();  // readers of the previous exchange are done
-#pragma unroll
-        for (int b = 0; b < (C::E >> PR); ++b)
-#pragma unroll
-            for (int q = 0; q < (1 << PR); ++q)
-                buf[swz(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP)] = v[b + q * (C::E >> PR)];
-        __syncthreads();
-#pragma unroll
-        for (int e = 0; e < C::E; ++e) v[e] = buf[swz(t + C::T * e, PP)];
-        subpass_run<LOGN, I>(v, t, tw);
-        RowsChain<LOGN, I + 1>::run(v, t, buf, tw);
-    }
-};
-template <int LOGN, int I>
-struct RowsChain<LOGN, I, true> {
-    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGN>::E], int, float2 *, const float2 *) {}
-};
-
 template <int LOGN>
 __global__ void __launch_bounds__(RowsCfg<LOGN>::THREADS, RowsCfg<LOGN>::MINB)
 fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                 float in_im_sign, float out_re_scale, float out_im_scale) {
     using C = RowsCfg<LOGN>;
     extern __shared__ float2 smem_rows[];
-    const int tid = threadIdx.x;
-    const int g = tid >> C::LOGT;
-    const int t = tid & (C::T - 1);
-    const uint64_t row = (uint64_t)blockIdx.x * C::G + g;
-    const bool active = row < batch;
-    const float2 *src = in + row * C::N;
-    float2 *dst = out + row * C::N;
-    float2 *buf = smem_rows + g * C::N;
-
-    float2 v[C::E];
-#pragma unroll
-    for (int e = 0; e < C::E; ++e) {
-        float2 x = active ? ld_stream(src + t + C::T * e) : make_float2(0.f, 0.f);
-        x.y *= in_im_sign;
-        v[e] = x;
-    }
-    subpass_run<LOGN, 0>(v, t, tw);
-    RowsChain<LOGN, 1>::run(v, t, buf, tw);
-
-    // Last sub-pass (p * R = N): output q of butterfly j sits at j + q p.
-    if (active) {
-        constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
-        constexpr int NB = C::E >> LR;
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-#pragma unroll
-            for (int q = 0; q < (1 << LR); ++q) {
-                const float2 y = v[b + q * NB];
-                st_stream(dst + subpass_out_pos<LR, LP, C::LOGT>(t, b, q),
-                          make_float2(y.x * out_re_scale, y.y * out_im_scale));
-            }
-    }
+    auto ref = [&](int g) {
+        const uint64_t row = (uint64_t)blockIdx.x * C::G + g;
+        return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale};
+    };
+    rows_tile<LOGN, C::G>(ref, tw, smem_rows);
 }
 
 // ---------------------------------------------------------------------------

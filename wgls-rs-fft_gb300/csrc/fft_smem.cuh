@@ -90,8 +90,12 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
             float2 x[R];
 #pragma unroll
             for (int m = 0; m < R; ++m) x[m] = v[b + m * NB];
+            auto apply = [&](auto mc) {
+                constexpr int M = decltype(mc)::value;
+                if constexpr (M > 0) x[M] = cmul(mul_w16c<FactoredTw<LOGE, LOGR, b, M>::idx16>(x[M]), wt[M]);
+            };
             [&]<int... Ms>(std::integer_sequence<int, Ms...>) {
-                ((Ms > 0 ? (x[Ms] = cmul(mul_w16c<FactoredTw<LOGE, LOGR, b, Ms>::idx16>(x[Ms]), wt[Ms]), 0) : 0), ...);
+                (apply(std::integral_constant<int, Ms>{}), ...);
             }(std::make_integer_sequence<int, R>{});
             Dft<R>::run(x);
 #pragma unroll

@@ -1,0 +1,219 @@
+// Tile bodies shared by the uniform kernels (fft_rows.cu, fft_passes.cu) and
+// the ragged persistent kernel (fft_ragged.cu).
+//
+//   rows_tile<LOGN, G>  -- G whole transforms of length 2^LOGN, one HBM read and
+//                          one HBM write per sample (the single-pass form).
+//   pass_tile<LOGR, NG, FIRST>
+//                       -- NG groups of 16 adjacent columns of one global
+//                          Stockham pass of radix R = 2^LOGR (multi-pass form).
+// Both use all G*T (resp. NG*16*T) threads of the CTA and __syncthreads().
+#pragma once
+#include "fft_smem.cuh"
+
+namespace gbfft {
+
+constexpr int kColsLog = 4;
+constexpr int kCols = 1 << kColsLog;
+
+__device__ __forceinline__ int swz(int a, int logp) {
+    return logp < 4 ? (a ^ (((a >> 4) << logp) & 15)) : a;
+}
+
+// Sub-passes 1..NSUB-1 of a row transform held as v[] by thread t, exchanged
+// through buf (XOR-swizzled positions).
+template <int LOGN, int I, bool DONE = (I >= SubCfg<LOGN>::NSUB)>
+struct RowsChain {
+    using C = SubCfg<LOGN>;
+    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, float2 *buf, const float2 *tw) {
+        constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);  // previous sub-pass
+        if (I > 1) __syncthreads();  // readers of the previous exchange are done
+#pragma unroll
+        for (int b = 0; b < (C::E >> PR); ++b)
+#pragma unroll
+            for (int q = 0; q < (1 << PR); ++q)
+                buf[swz(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP)] = v[b + q * (C::E >> PR)];
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < C::E; ++e) v[e] = buf[swz(t + C::T * e, PP)];
+        subpass_run<LOGN, I>(v, t, tw);
+        RowsChain<LOGN, I + 1>::run(v, t, buf, tw);
+    }
+};
+template <int LOGN, int I>
+struct RowsChain<LOGN, I, true> {
+    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGN>::E], int, float2 *, const float2 *) {}
+};
+
+// Per-transform access for rows_tile: where transform g of the tile lives,
+// whether it exists, and its direction.
+struct RowRef {
+    const float2 *src;
+    float2 *dst;
+    bool active;
+    float in_im, out_re, out_im;
+};
+
+// G transforms of length 2^LOGN; thread tid = g*T + t.  `ref(g)` gives the
+// transform's RowRef.  smem holds G*N complex values (unused if NSUB == 1).
+template <int LOGN, int G, class RefFn>
+__device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem) {
+    using C = SubCfg<LOGN>;
+    const int tid = threadIdx.x;
+    const int g = tid >> C::LOGT;
+    const int t = tid & (C::T - 1);
+    const RowRef r = ref(g);
+    float2 v[C::E];
+#pragma unroll
+    for (int e = 0; e < C::E; ++e) {
+        float2 x = r.active ? ld_stream(r.src + t + C::T * e) : make_float2(0.f, 0.f);
+        x.y *= r.in_im;
+        v[e] = x;
+    }
+    subpass_run<LOGN, 0>(v, t, tw);
+    RowsChain<LOGN, 1>::run(v, t, smem + g * C::N, tw);
+    // last sub-pass (p R = N): output q of butterfly j sits at j + q p
+    if (r.active) {
+        constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
+        constexpr int NB = C::E >> LR;
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+#pragma unroll
+            for (int q = 0; q < (1 << LR); ++q) {
+                const float2 y = v[b + q * NB];
+                st_stream(r.dst + subpass_out_pos<LR, LP, C::LOGT>(t, b, q), make_float2(y.x * r.out_re, y.y * r.out_im));
+            }
+    }
+}
+
+// ---- global-pass tiles -----------------------------------------------------
+
+template <int LOGR, int I, bool DONE = (I >= SubCfg<LOGR>::NSUB)>
+struct PassChain {
+    using C = SubCfg<LOGR>;
+    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, int c, float2 *buf, const float2 *tw) {
+        constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);
+        if (I > 1) __syncthreads();
+#pragma unroll
+        for (int b = 0; b < (C::E >> PR); ++b)
+#pragma unroll
+            for (int q = 0; q < (1 << PR); ++q)
+                buf[(subpass_out_pos<PR, PP, C::LOGT>(t, b, q) << kColsLog) + c] = v[b + q * (C::E >> PR)];
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < C::E; ++e) v[e] = buf[((t + C::T * e) << kColsLog) + c];
+        subpass_run<LOGR, I>(v, t, tw);
+        PassChain<LOGR, I + 1>::run(v, t, c, buf, tw);
+    }
+};
+template <int LOGR, int I>
+struct PassChain<LOGR, I, true> {
+    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR>::E], int, int, float2 *, const float2 *) {}
+};
+
+__device__ __forceinline__ float2 twiddle_2level(const float2 *__restrict__ lo, const float2 *__restrict__ hi,
+                                                 uint32_t ex, int split) {
+    return cmul(ld_tw(hi + (ex >> split)), ld_tw(lo + (ex & ((1u << split) - 1))));
+}
+
+template <int LOGR, int NG>
+struct PassTileCfg {
+    using S = SubCfg<LOGR>;
+    static constexpr int THREADS = NG * kCols * S::T;
+    static constexpr int COLTW_STRIDE = S::E + 1;  // padded: conflict-free column reads
+    static constexpr size_t SMEM_ELEMS = (size_t)NG * kCols * S::N + (size_t)NG * kCols * COLTW_STRIDE;
+};
+
+// Arguments of one global pass over one transform (offsets already applied).
+struct PassArgs {
+    const float2 *src;  // transform base, input of this pass
+    float2 *dst;        // transform base, output of this pass
+    int logn, logp;
+    uint32_t col0;      // first column of the tile (multiple of NG*16)
+    const float2 *tw_sub, *tw_lo, *tw_hi;
+    int tw_split;
+    float in_im, out_re, out_im;
+    bool coherent_load;  // input written earlier in the same kernel: bypass L1
+};
+
+// NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
+template <int LOGR, int NG, bool FIRST>
+__device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem) {
+    using C = SubCfg<LOGR>;
+    using K = PassTileCfg<LOGR, NG>;
+    constexpr int R = C::N, T = C::T, E = C::E;
+    const int tid = threadIdx.x;
+    const int grp = tid / (kCols * T);
+    const int lt = tid - grp * (kCols * T);
+    const int c = lt & (kCols - 1);
+    const int t = lt >> kColsLog;
+    float2 *buf = smem + grp * (kCols * R);
+    float2 *coltw = smem + NG * kCols * R + grp * (kCols * K::COLTW_STRIDE);
+    const int lognc = a.logn - LOGR;
+    const uint32_t j0 = a.col0 + grp * kCols;
+    const uint32_t j = j0 + c;
+
+    float2 v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+        const uint32_t m = t + T * e;
+        const float2 *p = a.src + j + ((uint64_t)m << lognc);
+        float2 x = a.coherent_load ? __ldcg(p) : ld_stream(p);
+        x.y *= a.in_im;
+        v[e] = x;
+    }
+    if (!FIRST) {
+        const uint32_t pmask = (1u << a.logp) - 1;
+        // per-column factors W_{E p}^{e k} = W_N^{(e k) << (logn - LOGE - logp)}
+        const int sh_col = a.logn - C::LOGE - a.logp;
+        for (int i = lt; i < kCols * E; i += kCols * T) {
+            const int cc = i >> C::LOGE, ee = i & (E - 1);
+            const uint32_t kk = (j0 + cc) & pmask;
+            coltw[cc * K::COLTW_STRIDE + ee] = twiddle_2level(a.tw_lo, a.tw_hi, (kk * ee) << sh_col, a.tw_split);
+        }
+        // per-thread factor W_{R p}^{t k}
+        const uint32_t k = j & pmask;
+        const float2 w = twiddle_2level(a.tw_lo, a.tw_hi, (t * k) << (a.logn - LOGR - a.logp), a.tw_split);
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = cmul(v[e], cmul(w, coltw[c * K::COLTW_STRIDE + e]));
+    }
+    subpass_run<LOGR, 0>(v, t, a.tw_sub);
+    PassChain<LOGR, 1>::run(v, t, c, buf, a.tw_sub);
+
+    constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
+    constexpr int NB = E >> LR;
+    if (FIRST) {
+        // Outputs of column j are contiguous at j R + q: stage them as
+        // [column][q ^ column] and store each group's 16 R-sample block linearly.
+        __syncthreads();
+#pragma unroll
+        for (int bb = 0; bb < NB; ++bb)
+#pragma unroll
+            for (int q = 0; q < (1 << LR); ++q) {
+                const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
+                buf[c * R + (pos ^ c)] = v[bb + q * NB];
+            }
+        __syncthreads();
+        float2 *blk = a.dst + (uint64_t)j0 * R;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const int lin = lt + kCols * T * e;
+            const int cc = lin >> LOGR, q = lin & (R - 1);
+            const float2 y = buf[cc * R + (q ^ cc)];
+            st_stream(blk + lin, make_float2(y.x * a.out_re, y.y * a.out_im));
+        }
+    } else {
+        const uint32_t pmask = (1u << a.logp) - 1;
+        float2 *col = a.dst + ((uint64_t)(j >> a.logp) << (LOGR + a.logp)) + (j & pmask);
+#pragma unroll
+        for (int bb = 0; bb < NB; ++bb)
+#pragma unroll
+            for (int q = 0; q < (1 << LR); ++q) {
+                const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
+                const float2 y = v[bb + q * NB];
+                st_stream(col + ((uint64_t)pos << a.logp), make_float2(y.x * a.out_re, y.y * a.out_im));
+            }
+    }
+}
+
+}  // namespace gbfft

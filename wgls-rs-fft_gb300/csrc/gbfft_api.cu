@@ -17,8 +17,14 @@
 
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"
+#include "gbfft_ragged.h"
 
 using namespace gbfft;
+
+struct gbfft_ragged_plan {
+    gbfft_ctx *ctx;
+    RaggedPlanImpl *impl;
+};
 
 struct gbfft_ctx {
     int device = 0;
@@ -321,6 +327,74 @@ int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows, const uint6
     if (st != GBFFT_OK) return st;
     for (uint64_t i = 0; i < batch; ++i) memcpy(out_rows[i], stage + i * row_bytes, row_bytes);
     return GBFFT_OK;
+}
+
+int gbfft_ragged_plan_create(gbfft_ctx *ctx, const gbfft_ragged_desc *descs, uint32_t count,
+                             gbfft_ragged_plan **out_plan) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (!out_plan || (count > 0 && !descs)) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null argument");
+    *out_plan = nullptr;
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    RaggedPlanImpl *impl = nullptr;
+    std::string why;
+    int st = ragged_plan_build(impl, ctx->device, descs, count, why);
+    if (st != GBFFT_OK) return fail(ctx, st, "%s", why.c_str());
+    *out_plan = new gbfft_ragged_plan{ctx, impl};
+    return GBFFT_OK;
+}
+
+int gbfft_ragged_plan_set(gbfft_ragged_plan *plan, int option, uint64_t value) {
+    if (!plan) return GBFFT_ERR_INVALID_ARGUMENT;
+    std::string why;
+    int st = ragged_plan_set(*plan->impl, option, value, why);
+    return st == GBFFT_OK ? st : fail(plan->ctx, st, "%s", why.c_str());
+}
+
+int gbfft_ragged_execute(gbfft_ragged_plan *plan, const void *d_in, void *d_out, uint64_t capacity, int use_graph,
+                         void *stream) {
+    if (!plan) return GBFFT_ERR_INVALID_ARGUMENT;
+    gbfft_ctx *ctx = plan->ctx;
+    if (ragged_plan_items(*plan->impl) > 0 && (!d_in || !d_out))
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null device pointer");
+    if (ragged_plan_extent(*plan->impl) > capacity)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "descriptors reach sample %llu, past the buffer capacity %llu",
+                    (unsigned long long)ragged_plan_extent(*plan->impl), (unsigned long long)capacity);
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::string why;
+    const uint64_t before = ragged_plan_launches(*plan->impl);
+    int st = ragged_plan_execute(*plan->impl, d_in, d_out, (cudaStream_t)stream, use_graph != 0, why);
+    ctx->launches += ragged_plan_launches(*plan->impl) - before;
+    return st == GBFFT_OK ? st : fail(ctx, st, "ragged execute: %s", why.c_str());
+}
+
+int gbfft_ragged_wait(gbfft_ragged_plan *plan, void *stream) {
+    if (!plan) return GBFFT_ERR_INVALID_ARGUMENT;
+    GB_CUDA(plan->ctx, cudaSetDevice(plan->ctx->device));
+    std::string why;
+    int st = ragged_plan_wait(*plan->impl, (cudaStream_t)stream, why);
+    return st == GBFFT_OK ? st : fail(plan->ctx, st, "%s", why.c_str());
+}
+
+uint64_t gbfft_ragged_launch_count(const gbfft_ragged_plan *plan) {
+    return plan ? ragged_plan_launches(*plan->impl) : 0;
+}
+
+void gbfft_ragged_plan_destroy(gbfft_ragged_plan *plan) {
+    if (!plan) return;
+    cudaSetDevice(plan->ctx->device);
+    ragged_plan_free(plan->impl);
+    delete plan;
+}
+
+int gbfft_ragged_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t capacity,
+                        const gbfft_ragged_desc *descs, uint32_t count, void *stream) {
+    gbfft_ragged_plan *plan = nullptr;
+    int st = gbfft_ragged_plan_create(ctx, descs, count, &plan);
+    if (st != GBFFT_OK) return st;
+    st = gbfft_ragged_execute(plan, d_in, d_out, capacity, 0, stream);
+    if (st == GBFFT_OK) st = gbfft_ragged_wait(plan, stream);
+    gbfft_ragged_plan_destroy(plan);
+    return st;
 }
 
 int gbfft_bench_device(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, int warmup, int iters,

@@ -42,6 +42,13 @@ SIGNATURES = {
     "gbfft_c2c_host_rows": (_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_u64), ctypes.POINTER(_vp), _u64, _int]),
     "gbfft_c2c_device": (_int, [_vp, _vp, _vp, _u64, _u64, _int, _vp]),
     "gbfft_c2c_device_noalloc": (_int, [_vp, _vp, _u64, _u64, _int, _vp]),
+    "gbfft_ragged_plan_create": (_int, [_vp, _vp, ctypes.c_uint32, ctypes.POINTER(_vp)]),
+    "gbfft_ragged_plan_set": (_int, [_vp, _int, _u64]),
+    "gbfft_ragged_execute": (_int, [_vp, _vp, _vp, _u64, _int, _vp]),
+    "gbfft_ragged_wait": (_int, [_vp, _vp]),
+    "gbfft_ragged_launch_count": (_u64, [_vp]),
+    "gbfft_ragged_plan_destroy": (None, [_vp]),
+    "gbfft_ragged_device": (_int, [_vp, _vp, _vp, _u64, _vp, ctypes.c_uint32, _vp]),
     "gbfft_bench_device": (_int, [_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_set_precision": (_int, [_vp, _int]),
     "gbfft_launch_count": (_u64, [_vp]),
@@ -178,3 +185,67 @@ class Context:
         sec = ctypes.c_double()
         self._check(self._L.gbfft_bench_device(self._h, n, batch, direction, warmup, iters, ctypes.byref(sec)))
         return sec.value
+
+    def ragged_plan(self, descs) -> "RaggedPlan":
+        return RaggedPlan(self, descs)
+
+    def ragged_device(self, d_in, d_out, capacity: int, descs, stream=None):
+        d = ragged_descs(descs)
+        s = 0 if stream is None else int(stream)
+        self._check(self._L.gbfft_ragged_device(self._h, _ptr(d_in), _ptr(d_out), capacity, d.ctypes.data,
+                                                len(d), s or None))
+
+
+# struct gbfft_ragged_desc { uint64_t offset; uint32_t log2n; int32_t direction; }
+RAGGED_DESC_DTYPE = np.dtype([("offset", "<u8"), ("log2n", "<u4"), ("direction", "<i4")])
+
+
+def ragged_descs(descs) -> np.ndarray:
+    """Descriptors as a contiguous gbfft_ragged_desc array.  Accepts such an
+    array or an iterable of (offset, log2n, direction) tuples."""
+    if isinstance(descs, np.ndarray) and descs.dtype == RAGGED_DESC_DTYPE:
+        return np.ascontiguousarray(descs)
+    return np.array([tuple(d) for d in descs], dtype=RAGGED_DESC_DTYPE)
+
+
+class RaggedPlan:
+    """A gbfft_ragged_plan: one persistent launch over mixed sizes/directions."""
+
+    def __init__(self, ctx: Context, descs):
+        self._ctx = ctx
+        self._L = ctx._L
+        self.descs = ragged_descs(descs)
+        h = _vp()
+        ctx._check(self._L.gbfft_ragged_plan_create(ctx.handle, self.descs.ctypes.data, len(self.descs),
+                                                    ctypes.byref(h)))
+        self._h = h
+
+    def set(self, option: int, value: int):
+        self._ctx._check(self._L.gbfft_ragged_plan_set(self._h, option, value))
+
+    def execute(self, d_in, d_out, capacity: int, use_graph: bool = True, stream=None):
+        s = 0 if stream is None else int(stream)
+        self._ctx._check(self._L.gbfft_ragged_execute(self._h, _ptr(d_in), _ptr(d_out), capacity,
+                                                      int(use_graph), s or None))
+
+    def wait(self, stream=None):
+        s = 0 if stream is None else int(stream)
+        self._ctx._check(self._L.gbfft_ragged_wait(self._h, s or None))
+
+    def launch_count(self) -> int:
+        return int(self._L.gbfft_ragged_launch_count(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gbfft_ragged_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+RAGGED_OPT_SPIN_LIMIT = 1
+RAGGED_OPT_TEST_DROP_PRODUCERS = 2

@@ -144,3 +144,19 @@ def uniform_c64_torch(batch: int, n: int, seed: int, device="cuda"):
             h = _hash_torch(st, seed, idx)
             out[a:b, st] = ((h >> 8).to(torch.float32) * 2.0 ** -24) * 2.0 - 1.0
     return torch.view_as_complex(out).reshape(batch, n)
+
+
+def ragged_set(count: int = 10000, seed: int = 5, lo: int = 8, hi: int = 18):
+    """The ragged workload: `count` transforms with log2 N uniform on
+    {lo..hi} (h(2, seed, i) mod (hi-lo+1)), direction forward/inverse 50/50
+    (bit 0 of h(3, seed, i)), packed back to back in descriptor order.
+    Returns (descriptor array, total samples)."""
+    from ._lib import FORWARD, INVERSE, RAGGED_DESC_DTYPE
+    idx = np.arange(count, dtype=np.uint64).astype(np.uint32)
+    logn = (lo + hash_np(2, seed, idx) % np.uint32(hi - lo + 1)).astype(np.uint32)
+    dirs = np.where((hash_np(3, seed, idx) & np.uint32(1)) == 0, FORWARD, INVERSE).astype(np.int32)
+    sizes = np.left_shift(np.uint64(1), logn.astype(np.uint64))
+    offsets = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.uint64)
+    d = np.empty(count, dtype=RAGGED_DESC_DTYPE)
+    d["offset"], d["log2n"], d["direction"] = offsets, logn, dirs
+    return d, int(sizes.sum())

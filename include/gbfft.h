@@ -49,7 +49,11 @@ typedef enum gbfft_status {
 
 /* Arithmetic used for the butterflies. */
 typedef enum gbfft_precision {
-    GBFFT_PREC_FP32 = 0 /* plain FP32 Stockham form */
+    GBFFT_PREC_FP32 = 0,      /* plain FP32 Stockham form (every size) */
+    GBFFT_PREC_TC_FP16 = 1,   /* radix-16 sub-DFTs as tcgen05 matrix products, FP16 hi+lo operands
+                                 (3 products), per-vector power-of-two scaling, FP32 accumulation;
+                                 multi-pass sizes N >= 2^15 */
+    GBFFT_PREC_TC_BF16X3 = 2  /* same with BF16 hi+lo operands */
 } gbfft_precision;
 
 typedef struct gbfft_ctx gbfft_ctx;

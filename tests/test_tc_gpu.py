@@ -1,0 +1,77 @@
+"""GPU: the split-precision tensor-core form (tcgen05), through the C ABI.
+
+Gates, stated where used:
+  * FP16 hi+lo (3 products, per-vector power-of-two scaling): relative L2 <= 2e-6
+    against FP64 -- the same gate as the FP32 form;
+  * BF16x3 (16-bit significand pairs): its measured error is about 6e-6, so it
+    is held to 2e-5 and reported, not claimed against the 2e-6 gate;
+  * both: max |a - b| <= 1e-3 against the reference path on the reference's
+    benchmark input (src/benchmark.rs:204-217, 272-297).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tc_ctx(lib_built):
+    import gbfft
+    ctx = gbfft.Context(0)
+    yield ctx
+    ctx.close()
+
+
+@pytest.mark.parametrize("logn,batch", [(15, 4), (16, 8), (17, 2), (20, 1), (22, 1)])
+def test_tc_fp16_vs_fp64(tc_ctx, oracle, logn, batch):
+    import gbfft
+    from gbfft import signals
+    tc_ctx.set_precision(gbfft.PREC_TC_FP16)
+    x = signals.normal_c64(batch, 1 << logn, seed=60 + logn)
+    for direction, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        y = tc_ctx.c2c_host(x, direction)
+        err = oracle.rel_l2(y, oracle.fft64(x, inverse=inv))
+        assert err <= 2e-6, (logn, inv, err)
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5)])
+def test_tc_tones_workload(tc_ctx, oracle, prec, tol):
+    """The split-form workload at reduced batch: 64 tones at seeded bins with
+    amplitudes 10^U[-3,3] and phases U[0, 2 pi), plus N(0, 1e-2) noise."""
+    import gbfft
+    from gbfft import signals
+    tc_ctx.set_precision(prec)
+    x = signals.tones_c64(16, 1 << 16, seed=4)
+    y = tc_ctx.c2c_host(x, gbfft.FORWARD)
+    err = oracle.rel_l2(y, oracle.fft64(x))
+    assert err <= tol, err
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_tc_reference_path_gate(tc_ctx, oracle, prec):
+    import gbfft
+    tc_ctx.set_precision(prec)
+    n = 1 << 16
+    t = np.arange(n, dtype=np.float64) / n
+    xb = np.tile((0.001 * t + 1j * 0.001 * np.sin(2 * np.pi * t)).astype(np.complex64), (2, 1))
+    for direction, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        y = tc_ctx.c2c_host(xb, direction)
+        assert oracle.max_abs_err(y, oracle.ref_fft(xb, inverse=inv, threads=2)) <= 1e-3
+
+
+def test_tc_matches_fp32_form_and_limits(tc_ctx, oracle):
+    import gbfft
+    from gbfft import signals
+    x = signals.uniform_c64(4, 1 << 16, seed=61)
+    tc_ctx.set_precision(gbfft.PREC_FP32)
+    y32 = tc_ctx.c2c_host(x, gbfft.FORWARD)
+    tc_ctx.set_precision(gbfft.PREC_TC_FP16)
+    ytc = tc_ctx.c2c_host(x, gbfft.FORWARD)
+    assert oracle.rel_l2(ytc, y32) <= 2e-6
+    with pytest.raises(gbfft.GbfftError) as e:  # single-pass sizes stay FP32-only
+        tc_ctx.c2c_host(signals.uniform_c64(2, 4096, seed=1), gbfft.FORWARD)
+    assert e.value.status == gbfft.ERR_UNSUPPORTED
+    with pytest.raises(gbfft.GbfftError) as e:
+        tc_ctx.set_precision(7)
+    assert e.value.status == gbfft.ERR_INVALID_ARGUMENT
+    tc_ctx.set_precision(gbfft.PREC_FP32)

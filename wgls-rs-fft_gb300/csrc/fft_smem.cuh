@@ -77,9 +77,16 @@ struct FactoredTw {
     static constexpr int idx16 = ((M * B) << (4 - LOGE)) & 15;
 };
 
+// Engine of the radix-R butterflies: FP32 in registers (DftRegs) or, for the
+// split-precision form, tensor-core matrix products (fft_tc.cuh).
+struct DftRegs {
+    template <int R>
+    __device__ __forceinline__ void run(float2 (&x)[R]) { Dft<R>::run(x); }
+};
+
 // Butterflies of one sub-pass on the register array v.
-template <int LOGE, int LOGR, int LOGP, int LOGT, bool FACT = false>
-__device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, const float2 *tw) {
+template <int LOGE, int LOGR, int LOGP, int LOGT, bool FACT = false, class Eng = DftRegs>
+__device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, const float2 *tw, Eng &eng) {
     constexpr int E = 1 << LOGE, R = 1 << LOGR, NB = E / R, P = 1 << LOGP, T = 1 << LOGT;
     if constexpr (FACT) {
         float2 wt[R];
@@ -97,7 +104,7 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
             [&]<int... Ms>(std::integer_sequence<int, Ms...>) {
                 (apply(std::integral_constant<int, Ms>{}), ...);
             }(std::make_integer_sequence<int, R>{});
-            Dft<R>::run(x);
+            eng.template run<R>(x);
 #pragma unroll
             for (int q = 0; q < R; ++q) v[b + q * NB] = x[q];
         };
@@ -116,7 +123,7 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
 #pragma unroll
                 for (int m = 1; m < R; ++m) x[m] = cmul(x[m], ld_tw(tw + (m - 1) * P + k));
             }
-            Dft<R>::run(x);
+            eng.template run<R>(x);
 #pragma unroll
             for (int q = 0; q < R; ++q) v[b + q * NB] = x[q];
         }
@@ -134,10 +141,11 @@ inline int subcfg_segments(TwiddleSegment *out, uint64_t base) {
 }
 
 // Sub-pass I of the schedule of SubCfg<LOGN> (twiddle table already offset).
-template <int LOGN, int I>
-__device__ __forceinline__ void subpass_run(float2 (&v)[SubCfg<LOGN>::E], int t, const float2 *tw_all) {
+template <int LOGN, int I, class Eng = DftRegs>
+__device__ __forceinline__ void subpass_run(float2 (&v)[SubCfg<LOGN>::E], int t, const float2 *tw_all, Eng &eng) {
     using C = SubCfg<LOGN>;
-    subpass_compute<C::LOGE, C::logr(I), C::logp(I), C::LOGT, C::factored(I)>(v, t, tw_all + C::tw_offset(I));
+    subpass_compute<C::LOGE, C::logr(I), C::logp(I), C::LOGT, C::factored(I), Eng>(v, t, tw_all + C::tw_offset(I),
+                                                                                     eng);
 }
 
 // Position (within the transform) of output q of butterfly slot b after

@@ -1,0 +1,240 @@
+// Tensor-core (tcgen05) 16-point DFTs for the split-precision form.
+//
+// Every thread of a tile owns one 16-point vector x (the E = 16 samples of a
+// radix-16 sub-pass).  A whole sub-pass is then one real matrix product per
+// 128 threads,
+//     D[128 x 32] = A[128 x 32] . G[32 x 32],
+// with A's row r = [Re x_0..15 | Im x_0..15] of thread r and
+//     G[e][q]      =  cos(2 pi q e / 16)   G[16+e][q]    = sin(2 pi q e / 16)
+//     G[e][16+q]   = -sin(2 pi q e / 16)   G[16+e][16+q] = cos(2 pi q e / 16)
+// so that D's row r = [Re X_0..15 | Im X_0..15], the forward DFT of x.
+//
+// Precision: A and G are split into 16-bit hi + lo parts (FP16 or BF16) and
+// D = Ah.Gh + Ah.Gl + Al.Gh is accumulated in FP32 in tensor memory (the
+// Al.Gl term is below the FP32 rounding of the result).  Each row is first
+// scaled by an exact power of two so that its largest component lies in
+// [1, 2): FP16's range then always suffices and hi + lo carry 22 significant
+// bits (BF16: 16 bits).
+//
+// Operands live in shared memory in the canonical K-major, no-swizzle layout
+// of the tcgen05 matrix descriptors: 8 x 8 16-bit core matrices of 128 bytes,
+// core matrix (row block i, K block j) at (i * 4 + j) * 128 bytes, so the
+// descriptor's leading-dimension offset (between K-adjacent core matrices) is
+// 128 bytes and its stride-dimension offset (between row-adjacent ones) 512.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace gbfft {
+
+constexpr int kTcRowBytes = 64;        // 32 16-bit values
+constexpr uint32_t kTcLbo = 128;       // bytes between K-adjacent core matrices
+constexpr uint32_t kTcSbo = 512;       // bytes between row-adjacent core matrices
+constexpr int kTcGBytes = 32 * kTcRowBytes;  // one 32 x 32 G part
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Byte offset of element (row, k) in a K-major no-swizzle operand with 32 K.
+__host__ __device__ __forceinline__ uint32_t tc_elem_offset(uint32_t row, uint32_t k) {
+    return ((row >> 3) * 4 + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+// tcgen05 shared-memory matrix descriptor (no swizzle, K-major).
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFF) >> 4);        // bits 0-13: start address / 16
+    d |= (uint64_t)(kTcLbo >> 4) << 16;             // bits 16-29: leading-dimension byte offset / 16
+    d |= (uint64_t)(kTcSbo >> 4) << 32;             // bits 32-45: stride-dimension byte offset / 16
+    d |= (uint64_t)1 << 46;                         // bits 46-47: descriptor version 1
+    return d;                                       // base offset 0, swizzle mode 0 (none)
+}
+
+// Instruction descriptor, kind::f16: D F32, A/B F16 (bf16 = false) or BF16,
+// both K-major, M = 128, N = 32.
+__host__ __device__ constexpr uint32_t tc_idesc(bool bf16) {
+    return (1u << 4)                          // D format: F32
+           | ((bf16 ? 1u : 0u) << 7)          // A format
+           | ((bf16 ? 1u : 0u) << 10)         // B format
+           | ((32u >> 3) << 17)               // N / 8
+           | ((128u >> 4) << 24);             // M / 16
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// One warp: allocate `ncols` TMEM columns, address written to *dst.
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.u32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// 32 consecutive TMEM columns of this thread's lane (32x32b shape).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+template <bool BF16>
+struct TcSplit {
+    __device__ __forceinline__ static void split(float x, uint16_t &hi, uint16_t &lo) {
+        if constexpr (BF16) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(x);
+            const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+            hi = __bfloat16_as_ushort(h);
+            lo = __bfloat16_as_ushort(l);
+        } else {
+            const __half h = __float2half_rn(x);
+            const __half l = __float2half_rn(x - __half2float(h));
+            hi = __half_as_ushort(h);
+            lo = __half_as_ushort(l);
+        }
+    }
+};
+
+// Per-CTA state of the tensor-core DFT.
+struct TcState {
+    uint8_t *a_hi;       // [threads rows][32] 16-bit, canonical layout
+    uint8_t *a_lo;
+    const uint8_t *g_hi; // [32][32]
+    const uint8_t *g_lo;
+    uint64_t *bar;       // MMA completion barrier
+    int *abort;          // shared flag: a completion wait gave up
+    uint32_t *err;       // global error flag (set on timeout)
+    uint32_t taddr;      // TMEM base (lane 0, first column)
+    uint32_t parity;     // phase of *bar expected by the next wait
+    uint32_t nmma;       // threads / 128
+    uint32_t spin_limit;
+};
+
+// Forward 16-point DFT of x (natural order in, natural order out) on the
+// tensor cores.  Must be called by all threads of the CTA at the same point.
+template <bool BF16>
+__device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
+    const uint32_t r = threadIdx.x;
+    // 1. exact power-of-two scaling: largest |component| to [1, 2)
+    float m = 0.f;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) m = fmaxf(m, fmaxf(fabsf(x[e].x), fabsf(x[e].y)));
+    int ex = 0;
+    if (m > 0.f) {
+        ex = (int)((__float_as_uint(m) >> 23) & 0xff) - 127;
+        ex = ex < -126 ? -126 : ex;
+    }
+    const float down = __uint_as_float((uint32_t)(127 - ex) << 23);  // 2^-ex (ex in [-126, 127])
+    // 2. split into hi/lo rows of A
+    uint32_t hi[16], lo[16];
+#pragma unroll
+    for (int e = 0; e < 16; e += 2) {
+        uint16_t h0, l0, h1, l1;
+        TcSplit<BF16>::split(x[e].x * down, h0, l0);
+        TcSplit<BF16>::split(x[e + 1].x * down, h1, l1);
+        hi[e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lo[e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        TcSplit<BF16>::split(x[e].y * down, h0, l0);
+        TcSplit<BF16>::split(x[e + 1].y * down, h1, l1);
+        hi[8 + e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+        lo[8 + e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+    }
+#pragma unroll
+    for (int kb = 0; kb < 4; ++kb) {  // 4 chunks of 8 K-values (16 bytes)
+        const uint32_t off = tc_elem_offset(r, kb * 8);
+        *(uint4 *)(s.a_hi + off) = make_uint4(hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
+        *(uint4 *)(s.a_lo + off) = make_uint4(lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+    }
+    fence_proxy_async_smem();  // generic-proxy writes -> visible to the tensor core
+    tc_fence_before();
+    __syncthreads();
+    // 3. one thread issues D = Ah.Gh + Ah.Gl + Al.Gh for every 128-row block
+    //    (skipped once any CTA of the launch has given up waiting)
+    if (r == 0) {
+        if (*(volatile uint32_t *)s.err != 0u) *s.abort = 1;
+        if (!*s.abort) {
+            tc_fence_after();
+            constexpr uint32_t idesc = tc_idesc(BF16);
+            const uint32_t ah = smem_u32(s.a_hi), al = smem_u32(s.a_lo);
+            const uint32_t gh = smem_u32(s.g_hi), gl = smem_u32(s.g_lo);
+            for (uint32_t mb = 0; mb < s.nmma; ++mb) {
+                const uint32_t d = s.taddr + mb * 32;
+                const uint32_t arow = mb * 128 * kTcRowBytes;  // 128 rows = 16 row blocks of 512 B
+                uint32_t acc = 0;
+#pragma unroll
+                for (int part = 0; part < 3; ++part) {
+                    const uint32_t a = (part == 2 ? al : ah) + arow;
+                    const uint32_t g = part == 1 ? gl : gh;
+#pragma unroll
+                    for (uint32_t ks = 0; ks < 2; ++ks) {  // K = 32 = 2 x 16
+                        tc_mma(d, tc_smem_desc(a + ks * 2 * kTcLbo), tc_smem_desc(g + ks * 2 * kTcLbo), idesc, acc);
+                        acc = 1;
+                    }
+                }
+            }
+            tc_commit(s.bar);
+            uint32_t polls = 0;
+            while (!mbar_try_wait(s.bar, s.parity)) {
+                if (++polls > s.spin_limit) {
+                    *s.abort = 1;
+                    atomicExch(s.err, 2u);
+                    break;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    s.parity ^= 1u;
+    // 4. read this thread's row back: lanes of warp (r / 32) % 4, columns of block r / 128
+    tc_fence_after();
+    uint32_t d[32];
+    const uint32_t taddr = s.taddr + ((((r >> 5) & 3) * 32) << 16) + (r >> 7) * 32;
+    tmem_ld32(taddr, d);
+    tc_fence_before();
+    const float up = __uint_as_float((uint32_t)(127 + ex) << 23);  // 2^ex
+#pragma unroll
+    for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]) * up, __uint_as_float(d[16 + q]) * up);
+}
+
+}  // namespace gbfft

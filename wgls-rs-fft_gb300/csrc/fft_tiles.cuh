@@ -24,7 +24,8 @@ __device__ __forceinline__ int swz(int a, int logp) {
 template <int LOGN, int I, bool DONE = (I >= SubCfg<LOGN>::NSUB)>
 struct RowsChain {
     using C = SubCfg<LOGN>;
-    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, float2 *buf, const float2 *tw) {
+    template <class Eng>
+    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, float2 *buf, const float2 *tw, Eng &eng) {
         constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);  // previous sub-pass
         if (I > 1) __syncthreads();  // readers of the previous exchange are done
 #pragma unroll
@@ -35,13 +36,14 @@ struct RowsChain {
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < C::E; ++e) v[e] = buf[swz(t + C::T * e, PP)];
-        subpass_run<LOGN, I>(v, t, tw);
-        RowsChain<LOGN, I + 1>::run(v, t, buf, tw);
+        subpass_run<LOGN, I>(v, t, tw, eng);
+        RowsChain<LOGN, I + 1>::run(v, t, buf, tw, eng);
     }
 };
 template <int LOGN, int I>
 struct RowsChain<LOGN, I, true> {
-    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGN>::E], int, float2 *, const float2 *) {}
+    template <class Eng>
+    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGN>::E], int, float2 *, const float2 *, Eng &) {}
 };
 
 // Per-transform access for rows_tile: where transform g of the tile lives,
@@ -55,8 +57,8 @@ struct RowRef {
 
 // G transforms of length 2^LOGN; thread tid = g*T + t.  `ref(g)` gives the
 // transform's RowRef.  smem holds G*N complex values (unused if NSUB == 1).
-template <int LOGN, int G, class RefFn>
-__device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem) {
+template <int LOGN, int G, class RefFn, class Eng = DftRegs>
+__device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem, Eng eng = Eng()) {
     using C = SubCfg<LOGN>;
     const int tid = threadIdx.x;
     const int g = tid >> C::LOGT;
@@ -69,8 +71,8 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
         x.y *= r.in_im;
         v[e] = x;
     }
-    subpass_run<LOGN, 0>(v, t, tw);
-    RowsChain<LOGN, 1>::run(v, t, smem + g * C::N, tw);
+    subpass_run<LOGN, 0>(v, t, tw, eng);
+    RowsChain<LOGN, 1>::run(v, t, smem + g * C::N, tw, eng);
     // last sub-pass (p R = N): output q of butterfly j sits at j + q p
     if (r.active) {
         constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
@@ -90,7 +92,9 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
 template <int LOGR, int I, bool DONE = (I >= SubCfg<LOGR>::NSUB)>
 struct PassChain {
     using C = SubCfg<LOGR>;
-    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, int c, float2 *buf, const float2 *tw) {
+    template <class Eng>
+    __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, int c, float2 *buf, const float2 *tw,
+                                               Eng &eng) {
         constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);
         if (I > 1) __syncthreads();
 #pragma unroll
@@ -101,13 +105,15 @@ struct PassChain {
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < C::E; ++e) v[e] = buf[((t + C::T * e) << kColsLog) + c];
-        subpass_run<LOGR, I>(v, t, tw);
-        PassChain<LOGR, I + 1>::run(v, t, c, buf, tw);
+        subpass_run<LOGR, I>(v, t, tw, eng);
+        PassChain<LOGR, I + 1>::run(v, t, c, buf, tw, eng);
     }
 };
 template <int LOGR, int I>
 struct PassChain<LOGR, I, true> {
-    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR>::E], int, int, float2 *, const float2 *) {}
+    template <class Eng>
+    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR>::E], int, int, float2 *, const float2 *,
+                                               Eng &) {}
 };
 
 __device__ __forceinline__ float2 twiddle_2level(const float2 *__restrict__ lo, const float2 *__restrict__ hi,
@@ -136,8 +142,8 @@ struct PassArgs {
 };
 
 // NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
-template <int LOGR, int NG, bool FIRST>
-__device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem) {
+template <int LOGR, int NG, bool FIRST, class Eng = DftRegs>
+__device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng eng = Eng()) {
     using C = SubCfg<LOGR>;
     using K = PassTileCfg<LOGR, NG>;
     constexpr int R = C::N, T = C::T, E = C::E;
@@ -177,8 +183,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem) {
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = cmul(v[e], cmul(w, coltw[c * K::COLTW_STRIDE + e]));
     }
-    subpass_run<LOGR, 0>(v, t, a.tw_sub);
-    PassChain<LOGR, 1>::run(v, t, c, buf, a.tw_sub);
+    subpass_run<LOGR, 0>(v, t, a.tw_sub, eng);
+    PassChain<LOGR, 1>::run(v, t, c, buf, a.tw_sub, eng);
 
     constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
     constexpr int NB = E >> LR;

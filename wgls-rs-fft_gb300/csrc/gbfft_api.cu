@@ -32,9 +32,10 @@ struct gbfft_ctx {
     cudaStream_t xfer[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
-    std::map<int, std::unique_ptr<Plan>> plans;
+    std::map<int, std::unique_ptr<Plan>> plans;  // key: logn + 64 * precision
     DeviceBuffer dbuf;    // device copy of a host batch
     DeviceBuffer ws;      // multi-pass workspace
+    uint32_t *d_err = nullptr;  // raised by tensor-core kernels when a bounded wait gives up
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
     uint64_t launches = 0;
@@ -108,20 +109,32 @@ int ensure_hstage(gbfft_ctx *ctx, size_t bytes) {
 }
 
 int get_plan(gbfft_ctx *ctx, int logn, Plan **out) {
-    auto it = ctx->plans.find(logn);
+    const int key = logn + 64 * ctx->precision;
+    auto it = ctx->plans.find(key);
     if (it != ctx->plans.end()) {
         *out = it->second.get();
         return GBFFT_OK;
     }
     std::unique_ptr<Plan> p(new Plan());
     std::string why;
-    int st = plan_build(*p, logn, ctx->stream, why);
+    int st = plan_build(*p, logn, ctx->precision, ctx->stream, why);
     if (st != GBFFT_OK) return fail(ctx, st, "plan for N=2^%d: %s", logn, why.c_str());
     // Tables are filled on the context's stream; transforms may run on any
     // stream, so finish the fill before the plan is used (once per size).
     GB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     *out = p.get();
-    ctx->plans[logn] = std::move(p);
+    ctx->plans[key] = std::move(p);
+    return GBFFT_OK;
+}
+
+// After a synchronisation: report (and clear) a device-side wait that gave up.
+int check_device_flag(gbfft_ctx *ctx) {
+    uint32_t v = 0;
+    GB_CUDA(ctx, cudaMemcpy(&v, ctx->d_err, sizeof v, cudaMemcpyDeviceToHost));
+    if (v != 0) {
+        GB_CUDA(ctx, cudaMemset(ctx->d_err, 0, sizeof v));
+        return fail(ctx, GBFFT_ERR_TIMEOUT, "a tensor-core completion wait gave up");
+    }
     return GBFFT_OK;
 }
 
@@ -143,7 +156,7 @@ int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64
     if (st != GBFFT_OK) return st;
     uint64_t launches = 0;
     std::string why;
-    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, stream, launches, why);
+    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why);
     ctx->launches += launches;
     if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
                                     (unsigned long long)batch, why.c_str());
@@ -199,6 +212,8 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
         if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return GBFFT_ERR_CUDA;
     if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
         return GBFFT_ERR_CUDA;
+    if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_OUT_OF_MEMORY;
+    if (cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_CUDA;
     *out_ctx = ctx.release();
     return GBFFT_OK;
 }
@@ -215,6 +230,7 @@ void gbfft_destroy(gbfft_ctx *ctx) {
     ctx->plans.clear();
     ctx->dbuf.release();
     ctx->ws.release();
+    if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->hstage) cudaFreeHost(ctx->hstage);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -228,8 +244,8 @@ uint64_t gbfft_launch_count(const gbfft_ctx *ctx) { return ctx ? ctx->launches :
 
 int gbfft_set_precision(gbfft_ctx *ctx, int precision) {
     if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
-    if (precision != GBFFT_PREC_FP32)
-        return fail(ctx, GBFFT_ERR_UNSUPPORTED, "precision %d is not provided", precision);
+    if (precision != GBFFT_PREC_FP32 && precision != GBFFT_PREC_TC_FP16 && precision != GBFFT_PREC_TC_BF16X3)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "precision %d is not a gbfft_precision", precision);
     ctx->precision = precision;
     return GBFFT_OK;
 }
@@ -286,6 +302,8 @@ static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t
         ++k;
     }
     for (auto s : ctx->xfer) GB_CUDA(ctx, cudaStreamSynchronize(s));
+    st = check_device_flag(ctx);
+    if (st != GBFFT_OK) return st;
     if (!pinned) memcpy(out, ctx->hstage, bytes);
     return GBFFT_OK;
 }
@@ -420,6 +438,8 @@ int gbfft_bench_device(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction
     }
     GB_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
     GB_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+    st = check_device_flag(ctx);
+    if (st != GBFFT_OK) return st;
     float ms = 0.f;
     GB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     *seconds_per_iter = (double)ms * 1e-3 / iters;

@@ -28,11 +28,13 @@ void DeviceBuffer::release() {
 
 Plan::~Plan() {
     if (tw) cudaFree(tw);
+    if (gtab) cudaFree(gtab);
 }
 
-// Split log2 N into global-pass radices 2^5..2^10, largest first.
-std::vector<int> split_passes(int logn) {
-    int p = (logn + 9) / 10;
+// Split log2 N into global-pass radices 2^5..2^max_logr, largest first, with
+// as few passes as that allows.
+std::vector<int> split_passes(int logn, int max_logr) {
+    int p = (logn + max_logr - 1) / max_logr;
     if (p < 2) p = 2;
     std::vector<int> parts(p, logn / p);
     for (int i = 0; i < logn % p; ++i) parts[i] += 1;
@@ -60,10 +62,16 @@ uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t of
     return off;
 }
 
-int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
+int plan_build(Plan &p, int logn, int precision, cudaStream_t stream, std::string &why) {
     p.logn = logn;
+    p.precision = precision;
     std::vector<TwiddleSegment> segs;
     cudaError_t e;
+    const bool tc = precision != GBFFT_PREC_FP32;
+    if (tc && logn <= kRowsMaxLogN) {
+        why = "the tensor-core split form covers N >= 2^15 (multi-pass transforms)";
+        return GBFFT_ERR_UNSUPPORTED;
+    }
     if (logn <= kRowsMaxLogN) {
         if (!rows_kernel_info(logn, p.rows)) {
             why = "no single-pass kernel";
@@ -78,12 +86,16 @@ int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
     } else {
         p.multipass = true;
         p.needs_workspace = true;
-        std::vector<int> parts = split_passes(logn);
+        // the split form's radix-2^10 tile would not fit in shared memory
+        std::vector<int> parts = split_passes(logn, tc ? 9 : 10);
         int logp = 0;
         for (size_t i = 0; i < parts.size(); ++i) {
             PassDesc d;
-            if (!pass_kernel_info(parts[i], i == 0, d)) {
-                why = "no pass kernel for radix 2^" + std::to_string(parts[i]);
+            const bool ok = tc ? pass_tc_kernel_info(parts[i], i == 0, precision == GBFFT_PREC_TC_BF16X3, d)
+                               : pass_kernel_info(parts[i], i == 0, d);
+            if (!ok) {
+                why = std::string("no ") + (tc ? "tensor-core " : "") + "pass kernel for radix 2^" +
+                      std::to_string(parts[i]);
                 return GBFFT_ERR_UNSUPPORTED;
             }
             if ((e = pass_prepare(d)) != cudaSuccess) {
@@ -95,6 +107,17 @@ int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
             p.passes.push_back(d);
         }
         p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
+        if (tc) {
+            if ((e = cudaMalloc(&p.gtab, kTcGtabBytes)) != cudaSuccess) {
+                cudaGetLastError();
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_OUT_OF_MEMORY;
+            }
+            if ((e = tc_gtab_fill(p.gtab, stream)) != cudaSuccess) {
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_CUDA;
+            }
+        }
     }
     if (p.tw_entries > 0) {
         if ((e = cudaMalloc(&p.tw, p.tw_entries * sizeof(float2))) != cudaSuccess) {
@@ -111,7 +134,7 @@ int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why) {
 }
 
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction, DeviceBuffer &ws,
-                 cudaStream_t stream, uint64_t &launches, std::string &why) {
+                 uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why) {
     launches = 0;
     if (batch == 0) return GBFFT_OK;
     cudaError_t e;
@@ -157,8 +180,12 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
         const float in_im = (i == 0 && inv) ? -1.0f : 1.0f;
         const float out_re = (i == np - 1) ? scale : 1.0f;
         const float out_im = (i == np - 1 && inv) ? -scale : 1.0f;
-        e = pass_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
-                        p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, stream);
+        if (d.tc)
+            e = pass_tc_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
+                               p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, p.gtab, err, stream);
+        else
+            e = pass_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
+                            p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, stream);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;

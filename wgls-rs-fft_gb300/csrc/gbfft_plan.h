@@ -31,10 +31,13 @@ struct PassDesc {
     TwiddleSegment segs[kMaxSub] = {};  // its in-SMEM sub-pass tables, offsets from 0
     int nseg = 0;
     int tw_entries = 0;
+    bool tc = false;                    // radix-16 butterflies on the tensor cores
 };
 
 struct Plan {
     int logn = 0;
+    int precision = GBFFT_PREC_FP32;
+    void *gtab = nullptr;  // tensor-core forms: the 32 x 32 DFT operand parts
     bool multipass = false;
     bool needs_workspace = false;
     RowsKernelInfo rows;
@@ -55,8 +58,18 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                         float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream);
 
-// log2 radices of the global passes for a multi-pass transform of 2^logn.
-std::vector<int> split_passes(int logn);
+// fft_passes_tc.cu (split-precision tensor-core form)
+bool pass_tc_kernel_info(int logr, bool first, bool bf16, PassDesc &d);
+cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
+                           const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
+                           float in_im_sign, float out_re_scale, float out_im_scale, const void *gtab,
+                           uint32_t *err, cudaStream_t stream);
+cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
+constexpr size_t kTcGtabBytes = 4 * 2048;
+
+// log2 radices (each <= max_logr) of the global passes for a multi-pass
+// transform of 2^logn.
+std::vector<int> split_passes(int logn, int max_logr = 10);
 
 // Append the twiddle segments of a multi-pass schedule (per-pass sub-pass
 // tables, then the two-level W_N table) starting at `offset`; fills the pass
@@ -65,8 +78,9 @@ std::vector<int> split_passes(int logn);
 uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t offset,
                             std::vector<TwiddleSegment> &segs, uint64_t &lo_off, uint64_t &hi_off, int &split);
 
-int plan_build(Plan &p, int logn, cudaStream_t stream, std::string &why);
+int plan_build(Plan &p, int logn, int precision, cudaStream_t stream, std::string &why);
+// `err` is a device flag the tensor-core kernels raise when a bounded wait gives up.
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,
-                 DeviceBuffer &ws, cudaStream_t stream, uint64_t &launches, std::string &why);
+                 DeviceBuffer &ws, uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why);
 
 }  // namespace gbfft

@@ -16,6 +16,8 @@ from .build import LIB_PATH
 FORWARD = -1
 INVERSE = +1
 PREC_FP32 = 0
+PREC_TC_FP16 = 1
+PREC_TC_BF16X3 = 2
 
 OK = 0
 ERR_INVALID_SIZE = 1

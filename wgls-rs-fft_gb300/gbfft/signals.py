@@ -146,6 +146,31 @@ def uniform_c64_torch(batch: int, n: int, seed: int, device="cuda"):
     return torch.view_as_complex(out).reshape(batch, n)
 
 
+def _tone_params(batch: int, n: int, seed: int, tones: int):
+    idx = np.arange(batch * tones, dtype=np.uint64).astype(np.uint32)
+    bins = (hash_np(4, seed, idx) % np.uint32(n)).astype(np.int64).reshape(batch, tones)
+    u_amp = (hash_np(5, seed, idx) >> np.uint32(8)).astype(np.float64) * 2.0 ** -24
+    u_ph = (hash_np(6, seed, idx) >> np.uint32(8)).astype(np.float64) * 2.0 ** -24
+    amp = (10.0 ** (6.0 * u_amp - 3.0)).reshape(batch, tones)      # log-uniform in [1e-3, 1e3]
+    ph = (2.0 * np.pi * u_ph).reshape(batch, tones)                # uniform in [0, 2 pi)
+    return bins, amp, ph
+
+
+def tones_c64(batch: int, n: int, seed: int, tones: int = 64, sigma: float = 1e-2) -> np.ndarray:
+    """[batch, n] complex64: per row `tones` complex exponentials at bins
+    h(4, seed, .) mod n with amplitudes 10^U[-3,3] (h(5, .)) and phases
+    U[0, 2 pi) (h(6, .)), built exactly in FP64 through the inverse DFT of
+    their spectrum, plus complex N(0, sigma) noise (normal_c64 with seed + 1000;
+    sigma is the standard deviation of each of re and im)."""
+    bins, amp, ph = _tone_params(batch, n, seed, tones)
+    spec = np.zeros((batch, n), dtype=np.complex128)
+    rows = np.repeat(np.arange(batch), tones)
+    np.add.at(spec, (rows, bins.ravel()), (n * amp * np.exp(1j * ph)).ravel())
+    x = np.fft.ifft(spec, axis=1)
+    x += sigma * normal_c64(batch, n, seed + 1000).astype(np.complex128)
+    return x.astype(np.complex64)
+
+
 def ragged_set(count: int = 10000, seed: int = 5, lo: int = 8, hi: int = 18):
     """The ragged workload: `count` transforms with log2 N uniform on
     {lo..hi} (h(2, seed, i) mod (hi-lo+1)), direction forward/inverse 50/50

@@ -47,6 +47,7 @@ WORKLOADS = {
     "n16384_b4096": (14, 4096, "normal", 2),
     "n65536_b4096": (16, 4096, "normal", 2),
     "n65536_b1024": (16, 1024, "normal", 2),
+    "tones_n65536_b4096": (16, 4096, "tones", 4),
     "n262144_b256": (18, 256, "normal", 2),
     "n4194304_b64": (22, 64, "normal", 3),
     "n16777216_b4": (24, 4, "normal", 3),
@@ -62,10 +63,11 @@ def rank_info():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def passes_for(logn: int) -> int:
+def passes_for(logn: int, precision: str = "fp32") -> int:
     if logn <= 14:
         return 1
-    return max(2, (logn + 9) // 10)
+    m = 10 if precision == "fp32" else 9
+    return max(2, (logn + m - 1) // m)
 
 
 def peaks():
@@ -149,8 +151,10 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_input(logn, batch, dist, seed, device):
+def make_input(logn, batch, dist, seed, device, ctx=None):
     from gbfft import signals
+    if dist == "tones":
+        return signals.tones_c64_torch(batch, 1 << logn, seed, ctx, device=device)
     if dist == "normal":
         return signals.normal_c64_torch(batch, 1 << logn, seed, device=device)
     return signals.uniform_c64_torch(batch, 1 << logn, seed, device=device)
@@ -319,6 +323,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ragged_c5"], default=DEFAULT_WORKLOAD)
+    ap.add_argument("--precision", choices=["fp32", "tc_fp16", "tc_bf16x3"], default="fp32")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -349,7 +354,9 @@ def main():
 
     logn, batch, distn, seed = WORKLOADS[workload]
     n = 1 << logn
-    x = make_input(logn, batch, distn, seed, dev)
+    x = make_input(logn, batch, distn, seed, dev, ctx)
+    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3}[args.precision]
+    ctx.set_precision(prec)
     y = torch.empty_like(x)
     z = torch.empty_like(x)
     stream = torch.cuda.current_stream(dev)
@@ -393,8 +400,12 @@ def main():
     peak, peak_kind = peaks()
     traffic = profile_traffic(workload)
 
-    # check the last step's roundtrip (cheap, catches a broken build)
+    # check the last step's roundtrip (cheap, catches a broken build), and the
+    # forward result of a few rows against a float64 FFT of the same rows
     rt = (torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x)).item()
+    rows = sorted({0, batch // 2, batch - 1})
+    ref64 = torch.fft.fft(x[rows].to(torch.complex128), dim=1)
+    acc = (torch.linalg.vector_norm(y[rows].to(torch.complex128) - ref64) / torch.linalg.vector_norm(ref64)).item()
 
     # end to end through the host C ABI from pinned memory
     e2e = None
@@ -434,10 +445,12 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded PCG hash, re/im iid " + ("N(0,1))" if distn == "normal" else "U[-1,1))"),
+            "data": "synthetic (seeded PCG hash, " + {"normal": "re/im iid N(0,1))", "uniform": "re/im iid U[-1,1))",
+                                                      "tones": "64 tones 10^U[-3,3] + N(0,1e-2) noise)"}[distn],
             "config": {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse",
-                       "placement": "out-of-place", "form": "fp32 single-pass" if logn <= 14 else
-                       f"fp32 {passes_for(logn)}-pass", "l2": "inputs (512 MB) larger than L2; no flush",
+                       "placement": "out-of-place", "precision": args.precision,
+                       "form": ("single-pass" if logn <= 14 else f"{passes_for(logn, args.precision)}-pass"),
+                       "l2": f"inputs ({8 * n * batch >> 20} MB) larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
@@ -447,6 +460,8 @@ def main():
             "gpu_launches": launches,
             "clocks": sampler.summary(),
             "roundtrip_rel_l2": rt,
+            "accuracy": {"precision": args.precision, "rel_l2_vs_fp64": acc, "rows": rows,
+                         "reference": "float64 torch.fft of the sampled rows (checker only)"},
         }
         print(json.dumps(line), flush=True)
     ctx.close()

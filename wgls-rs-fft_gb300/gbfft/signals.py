@@ -171,6 +171,25 @@ def tones_c64(batch: int, n: int, seed: int, tones: int = 64, sigma: float = 1e-
     return x.astype(np.complex64)
 
 
+def tones_c64_torch(batch: int, n: int, seed: int, ctx, tones: int = 64, sigma: float = 1e-2, device="cuda"):
+    """Device-side tones_c64: the tone spectrum is scattered in HBM and turned
+    into the time signal by this library's own FP32 inverse transform (which
+    divides by n, hence the n factor), then the same noise is added."""
+    import torch
+    from ._lib import INVERSE, PREC_FP32
+    bins, amp, ph = _tone_params(batch, n, seed, tones)
+    spec = torch.zeros(batch * n, dtype=torch.complex128, device=device)
+    flat = torch.from_numpy((np.arange(batch)[:, None] * n + bins).ravel()).to(device)
+    vals = torch.from_numpy((n * amp * np.exp(1j * ph)).ravel()).to(device)
+    spec.index_add_(0, flat, vals)
+    spec = spec.to(torch.complex64).reshape(batch, n)
+    x = torch.empty_like(spec)
+    ctx.set_precision(PREC_FP32)
+    ctx.c2c_device(spec, x, n, batch, INVERSE, stream=torch.cuda.current_stream().cuda_stream)
+    x += sigma * normal_c64_torch(batch, n, seed + 1000, device=device)
+    return x
+
+
 def ragged_set(count: int = 10000, seed: int = 5, lo: int = 8, hi: int = 18):
     """The ragged workload: `count` transforms with log2 N uniform on
     {lo..hi} (h(2, seed, i) mod (hi-lo+1)), direction forward/inverse 50/50

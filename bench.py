@@ -63,6 +63,25 @@ def rank_info():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(value: float, device) -> float:
+    """Largest `value` over all ranks (the job is as slow as its slowest
+    replica); the identity with one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return value
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank: float, seconds_local: float, device) -> float:
+    """Whole-job throughput: all ranks' units over the slowest rank's time."""
+    import torch.distributed as dist
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    return units_per_rank * world / max_over_ranks(seconds_local, device)
+
+
 def passes_for(logn: int, precision: str = "fp32") -> int:
     if logn <= 14:
         return 1
@@ -250,12 +269,8 @@ def run_ragged(args, ctx, dev, rank, world):
     ev1.record(stream)
     plan.wait(stream=sp)
     sampler.stop()
-    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
     launches = plan.launch_count() - l0
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     value = total * args.steps * world / (ms * 1e-3) / 1e9
 
     # uniform-batch comparison: same transforms regrouped by (size, direction)
@@ -385,11 +400,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     launches = ctx.launch_count() - launches0
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
     samples_per_step = 2 * n * batch
     value = samples_per_step * args.steps * world / (ms * 1e-3) / 1e9
 
@@ -421,11 +432,7 @@ def main():
         for _ in range(args.e2e_steps):
             ctx.c2c_host_ptr(hx.data_ptr(), hy.data_ptr(), n, batch, gbfft.FORWARD)
             ctx.c2c_host_ptr(hy.data_ptr(), hz.data_ptr(), n, batch, gbfft.INVERSE)
-        el = time.perf_counter() - t0
-        if world > 1:
-            t = torch.tensor([el], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            el = float(t.item())
+        el = max_over_ranks(time.perf_counter() - t0, dev)
         nbytes = 8 * n * batch
         e2e = {"value": samples_per_step * args.e2e_steps * world / el / 1e9, "unit": UNIT,
                "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,

@@ -1,0 +1,117 @@
+// C++ mirror of larsjoost/wgls-rs-fft's executor interface over the C ABI in
+// gbfft.h -- header-only, no CUDA headers needed.
+//
+//   trait FftExecutor { name, fft, ifft, as_any }        src/lib.rs:32-45
+//   GpuFft::new / fft / ifft / is_gpu_available / Default src/lib.rs:285-489, 946-950
+//
+// Batches are std::vector<std::vector<std::complex<float>>> (the reference's
+// &[Vec<Complex<f32>>]); failures throw gbfft::Error carrying the status and
+// the library's message -- including the reference's own two messages for a
+// non-power-of-two length and for rows of different lengths.  An empty batch
+// returns an empty batch.
+#pragma once
+#include <complex>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "gbfft.h"
+
+namespace gbfft {
+
+using Complex = std::complex<float>;
+using Batch = std::vector<std::vector<Complex>>;
+
+class Error : public std::runtime_error {
+   public:
+    Error(int status, const std::string &msg) : std::runtime_error(msg), status_(status) {}
+    int status() const { return status_; }
+
+   private:
+    int status_;
+};
+
+class FftExecutor {
+   public:
+    virtual ~FftExecutor() = default;
+    virtual std::string name() const = 0;
+    virtual Batch fft(const Batch &inputs) = 0;
+    virtual Batch ifft(const Batch &inputs) = 0;
+};
+
+class GpuFft : public FftExecutor {
+   public:
+    // GpuFft::new (src/lib.rs:285-330): throws when no usable GB300 exists.
+    explicit GpuFft(int device = 0) {
+        const int st = gbfft_create(device, &ctx_);
+        if (st != GBFFT_OK) throw Error(st, gbfft_status_string(st));
+    }
+    ~GpuFft() override { gbfft_destroy(ctx_); }
+    GpuFft(const GpuFft &) = delete;
+    GpuFft &operator=(const GpuFft &) = delete;
+    GpuFft(GpuFft &&o) noexcept : ctx_(std::exchange(o.ctx_, nullptr)) {}
+    GpuFft &operator=(GpuFft &&o) noexcept {
+        if (this != &o) {
+            gbfft_destroy(ctx_);
+            ctx_ = std::exchange(o.ctx_, nullptr);
+        }
+        return *this;
+    }
+
+    // GpuFft::is_gpu_available (src/lib.rs:381-389)
+    static bool is_gpu_available() { return gbfft_is_available() != 0; }
+
+    std::string name() const override { return "GB300 (sm_103a Stockham radix-16)"; }
+
+    // GpuFft::fft (src/lib.rs:433-438): forward, unscaled.
+    Batch fft(const Batch &inputs) override { return run(inputs, GBFFT_FORWARD); }
+    // GpuFft::ifft (src/lib.rs:483-488): inverse scaled by 1/N.
+    Batch ifft(const Batch &inputs) override { return run(inputs, GBFFT_INVERSE); }
+
+    // Device-resident transform (no reference counterpart): interleaved
+    // complex<float> device buffers, enqueued on `stream` (a cudaStream_t).
+    void fft_device(const void *d_in, void *d_out, uint64_t n, uint64_t batch, int direction,
+                    void *stream = nullptr) {
+        check(gbfft_c2c_device(ctx_, d_in, d_out, n, batch, direction, stream));
+    }
+
+    // GpuFftTrait::benchmark_gpu_only (src/lib.rs:673-707): seconds per transform.
+    double benchmark_gpu_only(uint64_t n, uint64_t batch, int warmup, int iters) {
+        double s = 0.0;
+        check(gbfft_bench_device(ctx_, n, batch, GBFFT_FORWARD, warmup, iters, &s));
+        return s;
+    }
+
+    void set_precision(int precision) { check(gbfft_set_precision(ctx_, precision)); }
+    gbfft_ctx *context() { return ctx_; }
+
+   private:
+    void check(int st) {
+        if (st != GBFFT_OK) {
+            const char *m = gbfft_last_error(ctx_);
+            throw Error(st, (m && *m) ? m : gbfft_status_string(st));
+        }
+    }
+
+    Batch run(const Batch &inputs, int direction) {
+        if (inputs.empty()) return {};  // src/lib.rs:522-524
+        const size_t b = inputs.size();
+        std::vector<const float *> in(b);
+        std::vector<uint64_t> len(b);
+        Batch out(b);
+        std::vector<float *> outp(b);
+        for (size_t i = 0; i < b; ++i) {
+            in[i] = reinterpret_cast<const float *>(inputs[i].data());
+            len[i] = inputs[i].size();
+            out[i].resize(inputs[i].size());
+            outp[i] = reinterpret_cast<float *>(out[i].data());
+        }
+        check(gbfft_c2c_host_rows(ctx_, in.data(), len.data(), outp.data(), b, direction));
+        return out;
+    }
+
+    gbfft_ctx *ctx_ = nullptr;
+};
+
+}  // namespace gbfft

@@ -180,6 +180,19 @@ int gbfft_bench_device(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction
 /* Select the butterfly arithmetic for later calls on `ctx`. */
 int gbfft_set_precision(gbfft_ctx *ctx, int precision);
 
+/* Autotuner (no reference counterpart; the reference's find_optimal_batch
+ * example only sweeps batch sizes, examples/find_optimal_batch.rs:28).  Times
+ * every plan variant for (n, batch, direction, current precision) -- global
+ * pass split and plain vs persistent tile-loop kernels -- on the context's own
+ * scratch buffers (caller data is never touched), keeps the fastest for later
+ * calls with that size, direction, precision and a batch of the same power of
+ * two, and writes the mean seconds per transform of the winner.  If the
+ * environment variable GBFFT_AUTOTUNE_CACHE names a file, results are loaded
+ * from it when a context is created and appended to it here.  Setting
+ * GBFFT_AUTOTUNE=1 makes the first call of every untuned combination tune
+ * itself. */
+int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *best_seconds);
+
 /* Number of kernel launches this context has issued since creation (all
  * entry points).  Lets callers count GPU work without a profiler. */
 uint64_t gbfft_launch_count(const gbfft_ctx *ctx);

@@ -20,6 +20,8 @@
 // The first factor is one lookup per thread; the second depends only on the
 // column and e, so the CTA builds it once into a padded 16 x 17 shared table.
 // Both come from two FP64-built tables (W_N^i for i < 2^s and W_N^{i 2^s}).
+#include <algorithm>
+
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"
 #include "fft_tiles.cuh"
@@ -59,6 +61,44 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
     pass_tile<LOGR, 1, FIRST>(a, smem_pass);
 }
 
+// Persistent variant: each CTA walks tiles blockIdx.x, +gridDim.x, ... and asks
+// L2 for the next tile's R row segments (128 bytes each, one per thread)
+// before computing the current one.
+template <int LOGR, bool FIRST>
+__global__ void __launch_bounds__(PassCfg<LOGR>::THREADS, PassCfg<LOGR>::MINB)
+fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
+                           const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
+                           float in_im_sign, float out_re_scale, float out_im_scale, uint64_t ntiles) {
+    extern __shared__ float2 smem_pass[];
+    constexpr int R = 1 << LOGR;
+    const int lognc = logn - LOGR;
+    const uint64_t tiles_per_row = 1ull << (lognc - kColsLog);
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t next = tile + gridDim.x;
+        if (next < ntiles) {
+            const float2 *nb = in + ((next / tiles_per_row) << logn) + ((next % tiles_per_row) << kColsLog);
+            for (int m = threadIdx.x; m < R; m += PassCfg<LOGR>::THREADS) prefetch_l2(nb + ((uint64_t)m << lognc));
+        }
+        const uint64_t b = tile / tiles_per_row;
+        PassArgs a;
+        a.src = in + (b << logn);
+        a.dst = out + (b << logn);
+        a.logn = logn;
+        a.logp = logp;
+        a.col0 = (uint32_t)((tile % tiles_per_row) << kColsLog);
+        a.tw_sub = tw;
+        a.tw_lo = tw_lo;
+        a.tw_hi = tw_hi;
+        a.tw_split = tw_split;
+        a.in_im = in_im_sign;
+        a.out_re = out_re_scale;
+        a.out_im = out_im_scale;
+        a.coherent_load = false;
+        pass_tile<LOGR, 1, FIRST>(a, smem_pass);
+        __syncthreads();  // shared memory is reused by the next tile
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -67,6 +107,8 @@ template <int LOGR>
 static void pass_describe(PassDesc &d, bool first) {
     using C = PassCfg<LOGR>;
     d.fn = first ? (const void *)fft_pass_kernel<LOGR, true> : (const void *)fft_pass_kernel<LOGR, false>;
+    d.fn_persistent = first ? (const void *)fft_pass_persistent_kernel<LOGR, true>
+                            : (const void *)fft_pass_persistent_kernel<LOGR, false>;
     d.threads = C::THREADS;
     d.smem = C::SMEM;
     d.cols = kCols;
@@ -86,19 +128,33 @@ bool pass_kernel_info(int logr, bool first, PassDesc &d) {
     }
 }
 
-cudaError_t pass_prepare(const PassDesc &d) {
-    if (d.smem > 48 * 1024)
-        return cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem);
-    return cudaSuccess;
+cudaError_t pass_prepare(PassDesc &d) {
+    cudaError_t e = cudaSuccess;
+    if (d.smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem);
+        if (e == cudaSuccess && d.fn_persistent)
+            e = cudaFuncSetAttribute(d.fn_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem);
+        if (e != cudaSuccess) return e;
+    }
+    if (!d.fn_persistent) return cudaSuccess;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.persist_ctas_per_sm, d.fn_persistent, d.threads, d.smem);
 }
 
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
-                        float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream) {
-    const uint64_t tiles = batch << (logn - d.logr - kColsLog);
+                        float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
+                        bool persistent, int sms) {
+    uint64_t tiles = batch << (logn - d.logr - kColsLog);
     if (tiles == 0) return cudaSuccess;
-    if (tiles > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     int logp = d.logp;
+    if (persistent && d.fn_persistent && d.persist_ctas_per_sm > 0 && sms > 0) {
+        const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)d.persist_ctas_per_sm * (uint64_t)sms);
+        void *args[] = {(void *)&in,    (void *)&out,   (void *)&logn,     (void *)&logp,
+                        (void *)&tw_sub, (void *)&tw_lo, (void *)&tw_hi,   (void *)&tw_split,
+                        (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale, (void *)&tiles};
+        return cudaLaunchKernel(d.fn_persistent, dim3((unsigned)grid), dim3(d.threads), args, d.smem, stream);
+    }
+    if (tiles > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     void *args[] = {(void *)&in,    (void *)&out,   (void *)&logn,     (void *)&logp,
                     (void *)&tw_sub, (void *)&tw_lo, (void *)&tw_hi,   (void *)&tw_split,
                     (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale};

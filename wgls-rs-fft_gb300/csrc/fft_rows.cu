@@ -16,6 +16,8 @@
 // Buffers written by a sub-pass with stride p < 16 are XOR swizzled
 // (a ^ ((a >> 4) * p & 15)); with that every exchange is free of bank
 // conflicts for N >= 256.
+#include <algorithm>
+
 #include "gbfft_internal.h"
 #include "fft_tiles.cuh"
 
@@ -45,6 +47,36 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
     rows_tile<LOGN, C::G>(ref, tw, smem_rows);
 }
 
+// Persistent variant for the sizes whose per-transform footprint allows only
+// one or two CTAs per SM (N = 2^12 .. 2^14): each CTA walks tiles
+// blockIdx.x, +gridDim.x, ... and, before computing a tile, asks L2 for the
+// next one (one 128-byte line per thread), so the HBM fetch of tile i+1
+// overlaps the shared-memory sub-passes of tile i.
+template <int LOGN>
+__global__ void __launch_bounds__(RowsCfg<LOGN>::THREADS, RowsCfg<LOGN>::MINB)
+fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
+                           float in_im_sign, float out_re_scale, float out_im_scale) {
+    using C = RowsCfg<LOGN>;
+    extern __shared__ float2 smem_rows[];
+    constexpr uint32_t kTileSamples = C::G * C::N;
+    constexpr uint32_t kLines = kTileSamples * sizeof(float2) / 128;
+    const uint64_t ntiles = (batch + C::G - 1) / C::G;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t next = tile + gridDim.x;
+        if (next < ntiles) {
+            const char *p = (const char *)(in + next * kTileSamples);
+            const uint64_t avail = (batch - next * C::G) * C::N * sizeof(float2) / 128;  // lines inside the batch
+            for (uint32_t l = threadIdx.x; l < kLines && l < avail; l += C::THREADS) prefetch_l2(p + (uint64_t)l * 128);
+        }
+        auto ref = [&](int g) {
+            const uint64_t row = tile * C::G + g;
+            return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale};
+        };
+        rows_tile<LOGN, C::G>(ref, tw, smem_rows);
+        __syncthreads();  // shared memory is reused by the next tile
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -53,6 +85,7 @@ template <int LOGN>
 static void rows_describe(RowsKernelInfo &k) {
     using C = RowsCfg<LOGN>;
     k.fn = (const void *)fft_rows_kernel<LOGN>;
+    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN>;
     k.threads = C::THREADS;
     k.transforms_per_cta = C::G;
     k.smem = C::SMEM;
@@ -73,16 +106,26 @@ bool rows_kernel_info(int logn, RowsKernelInfo &k) {
     }
 }
 
-cudaError_t rows_prepare(const RowsKernelInfo &k) {
-    if (k.smem > 48 * 1024)
-        return cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
-    return cudaSuccess;
+cudaError_t rows_prepare(RowsKernelInfo &k) {
+    cudaError_t e = cudaSuccess;
+    if (k.smem > 48 * 1024) {
+        e = cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k.fn_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k.persist_ctas_per_sm, k.fn_persistent, k.threads, k.smem);
 }
 
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
-                        const float2 *tw, int direction, int logn, cudaStream_t stream) {
+                        const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream) {
     if (batch == 0) return cudaSuccess;
-    const uint64_t ctas = (batch + k.transforms_per_cta - 1) / k.transforms_per_cta;
+    uint64_t ctas = (batch + k.transforms_per_cta - 1) / k.transforms_per_cta;
+    const void *fn = k.fn;
+    if (persistent && k.persist_ctas_per_sm > 0 && sms > 0) {
+        fn = k.fn_persistent;
+        ctas = std::min<uint64_t>(ctas, (uint64_t)k.persist_ctas_per_sm * (uint64_t)sms);
+    }
     if (ctas > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     const bool inv = direction == GBFFT_INVERSE;
     const float scale = inv ? ldexpf(1.0f, -logn) : 1.0f;
@@ -90,7 +133,7 @@ cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, 
     float out_re = scale, out_im = inv ? -scale : 1.0f;
     void *args[] = {(void *)&in, (void *)&out, (void *)&batch, (void *)&tw,
                     (void *)&in_im, (void *)&out_re, (void *)&out_im};
-    return cudaLaunchKernel(k.fn, dim3((unsigned)ctas), dim3(k.threads), args, k.smem, stream);
+    return cudaLaunchKernel(fn, dim3((unsigned)ctas), dim3(k.threads), args, k.smem, stream);
 }
 
 }  // namespace gbfft

@@ -9,10 +9,12 @@
 // plus the device-resident entry gbfft_c2c_device.
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "gbfft_internal.h"
@@ -32,7 +34,13 @@ struct gbfft_ctx {
     cudaStream_t xfer[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::string err;
-    std::map<int, std::unique_ptr<Plan>> plans;  // key: logn + 64 * precision
+    // plans by (logn, precision, variant); tuned variant by (logn, precision, direction, log2 batch)
+    std::map<std::tuple<int, int, PlanVariant>, std::unique_ptr<Plan>> plans;
+    std::map<std::tuple<int, int, int, int>, PlanVariant> tuned;
+    bool auto_tune = false;
+    bool tune_verbose = false;  // GBFFT_AUTOTUNE_VERBOSE=1: per-variant timings on stderr
+    std::string tune_cache;
+    DeviceBuffer tune_a, tune_b;  // scratch for the autotuner
     DeviceBuffer dbuf;    // device copy of a host batch
     DeviceBuffer ws;      // multi-pass workspace
     uint32_t *d_err = nullptr;  // raised by tensor-core kernels when a bounded wait gives up
@@ -108,8 +116,8 @@ int ensure_hstage(gbfft_ctx *ctx, size_t bytes) {
     return GBFFT_OK;
 }
 
-int get_plan(gbfft_ctx *ctx, int logn, Plan **out) {
-    const int key = logn + 64 * ctx->precision;
+int get_plan(gbfft_ctx *ctx, int logn, const PlanVariant &v, Plan **out) {
+    const auto key = std::make_tuple(logn, ctx->precision, v);
     auto it = ctx->plans.find(key);
     if (it != ctx->plans.end()) {
         *out = it->second.get();
@@ -117,7 +125,7 @@ int get_plan(gbfft_ctx *ctx, int logn, Plan **out) {
     }
     std::unique_ptr<Plan> p(new Plan());
     std::string why;
-    int st = plan_build(*p, logn, ctx->precision, ctx->stream, why);
+    int st = plan_build(*p, logn, ctx->precision, v, ctx->stream, why);
     if (st != GBFFT_OK) return fail(ctx, st, "plan for N=2^%d: %s", logn, why.c_str());
     // Tables are filled on the context's stream; transforms may run on any
     // stream, so finish the fill before the plan is used (once per size).
@@ -148,11 +156,39 @@ int validate_common(gbfft_ctx *ctx, uint64_t n, int direction) {
     return GBFFT_OK;
 }
 
-// Enqueue one transform of the whole device batch on `stream`.
-int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
-               cudaStream_t stream) {
+int log2floor(uint64_t b) {
+    int l = 0;
+    while (b > 1) {
+        b >>= 1;
+        ++l;
+    }
+    return l;
+}
+
+std::tuple<int, int, int, int> tune_key(gbfft_ctx *ctx, int logn, uint64_t batch, int direction) {
+    return std::make_tuple(logn, ctx->precision, direction, log2floor(batch));
+}
+
+int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *best_seconds);
+
+PlanVariant choose_variant(gbfft_ctx *ctx, int logn, uint64_t batch, int direction, int &st) {
+    st = GBFFT_OK;
+    auto it = ctx->tuned.find(tune_key(ctx, logn, batch, direction));
+    if (it != ctx->tuned.end()) return it->second;
+    if (ctx->auto_tune) {
+        double s = 0;
+        st = autotune(ctx, 1ull << logn, batch, direction, &s);
+        it = ctx->tuned.find(tune_key(ctx, logn, batch, direction));
+        if (st == GBFFT_OK && it != ctx->tuned.end()) return it->second;
+    }
+    return plan_candidates(logn, ctx->precision).front();
+}
+
+// Enqueue one transform of the whole device batch on `stream` with variant v.
+int run_variant(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
+                const PlanVariant &v, cudaStream_t stream) {
     Plan *plan = nullptr;
-    int st = get_plan(ctx, log2u(n), &plan);
+    int st = get_plan(ctx, log2u(n), v, &plan);
     if (st != GBFFT_OK) return st;
     uint64_t launches = 0;
     std::string why;
@@ -161,6 +197,89 @@ int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64
     if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
                                     (unsigned long long)batch, why.c_str());
     return GBFFT_OK;
+}
+
+// Time every candidate variant on scratch buffers; remember (and persist) the fastest.
+int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *best_seconds) {
+    const int logn = log2u(n);
+    const size_t bytes = (size_t)n * batch * sizeof(float2);
+    int st = ctx->tune_a.ensure(bytes, ctx->err);
+    if (st == GBFFT_OK) st = ctx->tune_b.ensure(bytes, ctx->err);
+    if (st != GBFFT_OK) return fail(ctx, st, "%s", ctx->err.c_str());
+    float2 *a = (float2 *)ctx->tune_a.ptr, *b = (float2 *)ctx->tune_b.ptr;
+    GB_CUDA(ctx, cudaMemsetAsync(a, 0, bytes, ctx->stream));
+    const int reps = bytes >= ((size_t)256 << 20) ? 3 : 10;
+    double best = 1e30;
+    PlanVariant best_v = plan_candidates(logn, ctx->precision).front();
+    for (const PlanVariant &v : plan_candidates(logn, ctx->precision)) {
+        for (int w = 0; w < 2; ++w) {
+            st = run_variant(ctx, a, b, n, batch, direction, v, ctx->stream);
+            if (st != GBFFT_OK) break;
+        }
+        if (st != GBFFT_OK) {
+            st = GBFFT_OK;  // a variant that cannot run is skipped
+            continue;
+        }
+        GB_CUDA(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+        for (int r = 0; r < reps; ++r) {
+            st = run_variant(ctx, a, b, n, batch, direction, v, ctx->stream);
+            if (st != GBFFT_OK) return st;
+        }
+        GB_CUDA(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+        GB_CUDA(ctx, cudaEventSynchronize(ctx->ev1));
+        float ms = 0.f;
+        GB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        const double s = (double)ms * 1e-3 / reps;
+        if (ctx->tune_verbose)
+            fprintf(stderr, "gbfft autotune N=2^%d batch=%llu dir=%d prec=%d max_logr=%d persistent=%d: %.3f us\n",
+                    logn, (unsigned long long)batch, direction, ctx->precision, v.max_logr, v.persistent ? 1 : 0,
+                    s * 1e6);
+        if (s < best) {
+            best = s;
+            best_v = v;
+        }
+    }
+    st = check_device_flag(ctx);
+    if (st != GBFFT_OK) return st;
+    ctx->tuned[tune_key(ctx, logn, batch, direction)] = best_v;
+    if (best_seconds) *best_seconds = best;
+    if (!ctx->tune_cache.empty()) {
+        FILE *f = fopen(ctx->tune_cache.c_str(), "a");
+        if (f) {
+            fprintf(f,
+                    "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
+                    "\"max_logr\": %d, \"persistent\": %d, \"seconds\": %.9g}\n",
+                    logn, ctx->precision, direction, log2floor(batch), best_v.max_logr, best_v.persistent ? 1 : 0,
+                    best);
+            fclose(f);
+        }
+    }
+    return GBFFT_OK;
+}
+
+void load_tune_cache(gbfft_ctx *ctx) {
+    FILE *f = fopen(ctx->tune_cache.c_str(), "r");
+    if (!f) return;
+    char line[512];
+    while (fgets(line, sizeof line, f)) {
+        int logn, prec, dir, blog, mlr, pers;
+        double sec;
+        if (sscanf(line,
+                   "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
+                   "\"max_logr\": %d, \"persistent\": %d, \"seconds\": %lf}",
+                   &logn, &prec, &dir, &blog, &mlr, &pers, &sec) == 7)
+            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] = PlanVariant{mlr, pers != 0};
+    }
+    fclose(f);
+}
+
+// Enqueue one transform of the whole device batch on `stream`.
+int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
+               cudaStream_t stream) {
+    int st = GBFFT_OK;
+    const PlanVariant v = choose_variant(ctx, log2u(n), batch, direction, st);
+    if (st != GBFFT_OK) return st;
+    return run_variant(ctx, in, out, n, batch, direction, v, stream);
 }
 
 }  // namespace
@@ -214,6 +333,12 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
         return GBFFT_ERR_CUDA;
     if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_OUT_OF_MEMORY;
     if (cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_CUDA;
+    if (const char *c = getenv("GBFFT_AUTOTUNE_CACHE")) {
+        ctx->tune_cache = c;
+        load_tune_cache(ctx.get());
+    }
+    if (const char *a = getenv("GBFFT_AUTOTUNE")) ctx->auto_tune = a[0] == '1';
+    if (const char *a = getenv("GBFFT_AUTOTUNE_VERBOSE")) ctx->tune_verbose = a[0] == '1';
     *out_ctx = ctx.release();
     return GBFFT_OK;
 }
@@ -241,6 +366,14 @@ void gbfft_destroy(gbfft_ctx *ctx) {
 const char *gbfft_last_error(const gbfft_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
 
 uint64_t gbfft_launch_count(const gbfft_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *best_seconds) {
+    int st = validate_common(ctx, n, direction);
+    if (st != GBFFT_OK) return st;
+    if (batch == 0) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "batch must be positive");
+    GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    return autotune(ctx, n, batch, direction, best_seconds);
+}
 
 int gbfft_set_precision(gbfft_ctx *ctx, int precision) {
     if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
@@ -280,13 +413,10 @@ static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t
     // Split the batch into chunks of whole transforms and pipeline
     // H2D -> transform -> D2H over three streams so the two copy directions and
     // the kernels overlap.
-    Plan *plan = nullptr;
-    st = get_plan(ctx, log2u(n), &plan);
-    if (st != GBFFT_OK) return st;
     const size_t row_bytes = (size_t)n * sizeof(float2);
     const size_t chunk_target = (size_t)32 << 20;
     uint64_t rows_per_chunk = row_bytes >= chunk_target ? 1 : chunk_target / row_bytes;
-    if (plan->needs_workspace) rows_per_chunk = batch;  // one workspace: no overlap
+    if (log2u(n) > kRowsMaxLogN) rows_per_chunk = batch;  // multi-pass shares one workspace: no overlap
     uint64_t done = 0;
     int k = 0;
     while (done < batch) {

@@ -31,6 +31,8 @@ cudaError_t twiddle_fill(float2 *table, const TwiddleSegment *segs, int nseg, cu
 // ---- single-pass kernel (fft_rows.cu) ------------------------------------
 struct RowsKernelInfo {
     const void *fn = nullptr;
+    const void *fn_persistent = nullptr;  // tile loop with L2 prefetch of the next tile
+    int persist_ctas_per_sm = 0;          // resident CTAs of fn_persistent (set by rows_prepare)
     int threads = 0;
     int transforms_per_cta = 0;
     size_t smem = 0;
@@ -39,8 +41,9 @@ struct RowsKernelInfo {
     int tw_entries = 0;
 };
 bool rows_kernel_info(int logn, RowsKernelInfo &k);
-cudaError_t rows_prepare(const RowsKernelInfo &k);
+cudaError_t rows_prepare(RowsKernelInfo &k);
+// persistent: use fn_persistent with at most persist_ctas_per_sm * sms CTAs.
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
-                        const float2 *tw, int direction, int logn, cudaStream_t stream);
+                        const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream);
 
 }  // namespace gbfft

@@ -62,9 +62,34 @@ uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t of
     return off;
 }
 
-int plan_build(Plan &p, int logn, int precision, cudaStream_t stream, std::string &why) {
+std::vector<PlanVariant> plan_candidates(int logn, int precision) {
+    std::vector<PlanVariant> c;
+    if (logn <= kRowsMaxLogN) {
+        // one CTA per SM leaves no other CTA to overlap with: prefetch helps
+        const bool big = logn >= 13;
+        c.push_back(PlanVariant{10, big});
+        c.push_back(PlanVariant{10, !big});
+        return c;
+    }
+    const bool tc = precision != GBFFT_PREC_FP32;
+    const int top = tc ? 9 : 10;
+    for (int m = top; m >= 7; --m) {
+        const std::vector<int> parts = split_passes(logn, m);
+        bool dup = false;
+        for (const PlanVariant &v : c) dup |= split_passes(logn, v.max_logr) == parts;
+        if (dup || parts[0] < 5) continue;
+        c.push_back(PlanVariant{m, false});
+        if (!tc) c.push_back(PlanVariant{m, true});
+    }
+    return c;
+}
+
+int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStream_t stream, std::string &why) {
     p.logn = logn;
     p.precision = precision;
+    p.variant = v;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, dev);
     std::vector<TwiddleSegment> segs;
     cudaError_t e;
     const bool tc = precision != GBFFT_PREC_FP32;
@@ -87,7 +112,7 @@ int plan_build(Plan &p, int logn, int precision, cudaStream_t stream, std::strin
         p.multipass = true;
         p.needs_workspace = true;
         // the split form's radix-2^10 tile would not fit in shared memory
-        std::vector<int> parts = split_passes(logn, tc ? 9 : 10);
+        std::vector<int> parts = split_passes(logn, tc ? std::min(9, v.max_logr) : v.max_logr);
         int logp = 0;
         for (size_t i = 0; i < parts.size(); ++i) {
             PassDesc d;
@@ -139,7 +164,7 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
     if (batch == 0) return GBFFT_OK;
     cudaError_t e;
     if (!p.multipass) {
-        e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, stream);
+        e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.variant.persistent, p.sms, stream);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;
@@ -185,7 +210,8 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
                                p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, p.gtab, err, stream);
         else
             e = pass_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
-                            p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, stream);
+                            p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, stream, p.variant.persistent,
+                            p.sms);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;

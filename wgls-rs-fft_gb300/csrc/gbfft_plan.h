@@ -22,6 +22,8 @@ struct DeviceBuffer {
 // One global Stockham pass of the multi-pass form (fft_passes.cu).
 struct PassDesc {
     const void *fn = nullptr;
+    const void *fn_persistent = nullptr;  // tile loop with L2 prefetch of the next tile (FP32 form)
+    int persist_ctas_per_sm = 0;
     int logr = 0;        // transform size handled in shared memory: R = 2^logr
     int logp = 0;        // product of the radices of earlier global passes
     int cols = 0;        // columns (independent length-R DFTs) per CTA
@@ -34,8 +36,21 @@ struct PassDesc {
     bool tc = false;                    // radix-16 butterflies on the tensor cores
 };
 
+// The tunable choices of a plan: largest global-pass radix (multi-pass split)
+// and whether kernels run as persistent tile loops with L2 prefetch.
+struct PlanVariant {
+    int max_logr = 10;
+    bool persistent = false;
+    bool operator<(const PlanVariant &o) const {
+        return max_logr != o.max_logr ? max_logr < o.max_logr : persistent < o.persistent;
+    }
+    bool operator==(const PlanVariant &o) const { return max_logr == o.max_logr && persistent == o.persistent; }
+};
+
 struct Plan {
     int logn = 0;
+    PlanVariant variant;
+    int sms = 0;
     int precision = GBFFT_PREC_FP32;
     void *gtab = nullptr;  // tensor-core forms: the 32 x 32 DFT operand parts
     bool multipass = false;
@@ -53,10 +68,11 @@ struct Plan {
 
 // fft_passes.cu
 bool pass_kernel_info(int logr, bool first, PassDesc &d);
-cudaError_t pass_prepare(const PassDesc &d);
+cudaError_t pass_prepare(PassDesc &d);
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
-                        float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream);
+                        float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
+                        bool persistent = false, int sms = 0);
 
 // fft_passes_tc.cu (split-precision tensor-core form)
 bool pass_tc_kernel_info(int logr, bool first, bool bf16, PassDesc &d);
@@ -78,7 +94,11 @@ std::vector<int> split_passes(int logn, int max_logr = 10);
 uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t offset,
                             std::vector<TwiddleSegment> &segs, uint64_t &lo_off, uint64_t &hi_off, int &split);
 
-int plan_build(Plan &p, int logn, int precision, cudaStream_t stream, std::string &why);
+// Candidate variants the tuner tries for a size and precision, the first being
+// the default used before any tuning.
+std::vector<PlanVariant> plan_candidates(int logn, int precision);
+
+int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStream_t stream, std::string &why);
 // `err` is a device flag the tensor-core kernels raise when a bounded wait gives up.
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,
                  DeviceBuffer &ws, uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why);

@@ -53,6 +53,7 @@ SIGNATURES = {
     "gbfft_ragged_device": (_int, [_vp, _vp, _vp, _u64, _vp, ctypes.c_uint32, _vp]),
     "gbfft_bench_device": (_int, [_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_set_precision": (_int, [_vp, _int]),
+    "gbfft_autotune": (_int, [_vp, _u64, _u64, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_launch_count": (_u64, [_vp]),
     "gbfft_version": (ctypes.c_char_p, []),
 }
@@ -186,6 +187,13 @@ class Context:
     def bench_device(self, n: int, batch: int, direction: int = FORWARD, warmup: int = 3, iters: int = 20) -> float:
         sec = ctypes.c_double()
         self._check(self._L.gbfft_bench_device(self._h, n, batch, direction, warmup, iters, ctypes.byref(sec)))
+        return sec.value
+
+    def autotune(self, n: int, batch: int, direction: int = FORWARD) -> float:
+        """Time every plan variant for (n, batch, direction, precision); the
+        fastest serves later calls.  Returns its seconds per transform."""
+        sec = ctypes.c_double()
+        self._check(self._L.gbfft_autotune(self._h, n, batch, direction, ctypes.byref(sec)))
         return sec.value
 
     def ragged_plan(self, descs) -> "RaggedPlan":

@@ -339,6 +339,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ragged_c5"], default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", choices=["fp32", "tc_fp16", "tc_bf16x3"], default="fp32")
+    ap.add_argument("--window", choices=["none", "hann"], default="none",
+                    help="Hann window fused into every transform's load")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -372,6 +374,7 @@ def main():
     x = make_input(logn, batch, distn, seed, dev, ctx)
     prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3}[args.precision]
     ctx.set_precision(prec)
+    ctx.set_window(gbfft.WINDOW_HANN if args.window == "hann" else gbfft.WINDOW_NONE)
     y = torch.empty_like(x)
     z = torch.empty_like(x)
     stream = torch.cuda.current_stream(dev)
@@ -415,7 +418,12 @@ def main():
     # forward result of a few rows against a float64 FFT of the same rows
     rt = (torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x)).item()
     rows = sorted({0, batch // 2, batch - 1})
-    ref64 = torch.fft.fft(x[rows].to(torch.complex128), dim=1)
+    xr = x[rows].to(torch.complex128)
+    if args.window == "hann":  # the fused window multiplies every loaded sample
+        from gbfft import signals
+        xr = xr * torch.from_numpy(signals.hann_window(n).astype("float64")).to(dev)[None, :]
+        rt = None              # both directions load through the window: no roundtrip identity
+    ref64 = torch.fft.fft(xr, dim=1)
     acc = (torch.linalg.vector_norm(y[rows].to(torch.complex128) - ref64) / torch.linalg.vector_norm(ref64)).item()
 
     # end to end through the host C ABI from pinned memory
@@ -455,7 +463,7 @@ def main():
             "data": "synthetic (seeded PCG hash, " + {"normal": "re/im iid N(0,1))", "uniform": "re/im iid U[-1,1))",
                                                       "tones": "64 tones 10^U[-3,3] + N(0,1e-2) noise)"}[distn],
             "config": {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse",
-                       "placement": "out-of-place", "precision": args.precision,
+                       "placement": "out-of-place", "precision": args.precision, "window": args.window,
                        "form": ("single-pass" if logn <= 14 else f"{passes_for(logn, args.precision)}-pass"),
                        "l2": f"inputs ({8 * n * batch >> 20} MB) larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},

@@ -180,6 +180,17 @@ int gbfft_bench_device(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction
 /* Select the butterfly arithmetic for later calls on `ctx`. */
 int gbfft_set_precision(gbfft_ctx *ctx, int precision);
 
+/* Window applied to every input sample as the transform loads it (fused: no
+ * extra pass over memory).  GBFFT_WINDOW_HANN multiplies sample n of each
+ * length-N row by w_n = 0.5 (1 - cos(2 pi n / (N - 1))) -- the reference's
+ * host-side Hann window (tests/test_utils.rs:39-48, examples/windowed_fft.rs:
+ * 14-23) -- with w computed in FP64 and rounded once to f32; N = 1 uses w = 1.
+ * Applies to later gbfft_c2c_host / _host_rows / _device calls on `ctx` with
+ * N <= 2^24 (larger N returns GBFFT_ERR_UNSUPPORTED while a window is set). */
+#define GBFFT_WINDOW_NONE 0
+#define GBFFT_WINDOW_HANN 1
+int gbfft_set_window(gbfft_ctx *ctx, int window);
+
 /* Autotuner (no reference counterpart; the reference's find_optimal_batch
  * example only sweeps batch sizes, examples/find_optimal_batch.rs:28).  Times
  * every plan variant for (n, batch, direction, current precision) -- global

@@ -53,6 +53,7 @@ struct RowRef {
     float2 *dst;
     bool active;
     float in_im, out_re, out_im;
+    const float *win;  // window multiplied into each loaded sample, or nullptr
 };
 
 // G transforms of length 2^LOGN; thread tid = g*T + t.  `ref(g)` gives the
@@ -70,6 +71,13 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
         float2 x = r.active ? ld_stream(r.src + t + C::T * e) : make_float2(0.f, 0.f);
         x.y *= r.in_im;
         v[e] = x;
+    }
+    if (r.win != nullptr) {
+#pragma unroll
+        for (int e = 0; e < C::E; ++e) {
+            const float w = __ldg(r.win + t + C::T * e);
+            v[e] = make_float2(v[e].x * w, v[e].y * w);
+        }
     }
     subpass_run<LOGN, 0>(v, t, tw, eng);
     RowsChain<LOGN, 1>::run(v, t, smem + g * C::N, tw, eng);
@@ -139,6 +147,7 @@ struct PassArgs {
     int tw_split;
     float in_im, out_re, out_im;
     bool coherent_load;  // input written earlier in the same kernel: bypass L1
+    const float *win;    // first pass: window multiplied into each loaded sample, or nullptr
 };
 
 // NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
@@ -166,6 +175,13 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
         float2 x = a.coherent_load ? __ldcg(p) : ld_stream(p);
         x.y *= a.in_im;
         v[e] = x;
+    }
+    if (FIRST && a.win != nullptr) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const float w = __ldg(a.win + j + ((uint64_t)(t + T * e) << lognc));
+            v[e] = make_float2(v[e].x * w, v[e].y * w);
+        }
     }
     if (!FIRST) {
         const uint32_t pmask = (1u << a.logp) - 1;

@@ -37,6 +37,8 @@ struct gbfft_ctx {
     // plans by (logn, precision, variant); tuned variant by (logn, precision, direction, log2 batch)
     std::map<std::tuple<int, int, PlanVariant>, std::unique_ptr<Plan>> plans;
     std::map<std::tuple<int, int, int, int>, PlanVariant> tuned;
+    int window = GBFFT_WINDOW_NONE;
+    std::map<int, std::unique_ptr<DeviceBuffer>> windows;  // Hann tables by log2 N
     bool auto_tune = false;
     bool tune_verbose = false;  // GBFFT_AUTOTUNE_VERBOSE=1: per-variant timings on stderr
     std::string tune_cache;
@@ -153,6 +155,8 @@ int validate_common(gbfft_ctx *ctx, uint64_t n, int direction) {
     if (!is_pow2(n)) return fail(ctx, GBFFT_ERR_INVALID_SIZE, "%s", kMsgInvalidSize);
     if (log2u(n) > kMaxLogN)
         return fail(ctx, GBFFT_ERR_UNSUPPORTED, "transform length 2^%d exceeds 2^%d", log2u(n), kMaxLogN);
+    if (ctx->window != GBFFT_WINDOW_NONE && log2u(n) > kWindowMaxLogN)
+        return fail(ctx, GBFFT_ERR_UNSUPPORTED, "windows are provided for N <= 2^%d", kWindowMaxLogN);
     return GBFFT_OK;
 }
 
@@ -184,15 +188,37 @@ PlanVariant choose_variant(gbfft_ctx *ctx, int logn, uint64_t batch, int directi
     return plan_candidates(logn, ctx->precision).front();
 }
 
+// The window table for 2^logn samples when a window is selected, else nullptr.
+int window_table(gbfft_ctx *ctx, int logn, const float **out) {
+    *out = nullptr;
+    if (ctx->window == GBFFT_WINDOW_NONE) return GBFFT_OK;
+    if (logn > kWindowMaxLogN)
+        return fail(ctx, GBFFT_ERR_UNSUPPORTED, "windows are provided for N <= 2^%d", kWindowMaxLogN);
+    auto it = ctx->windows.find(logn);
+    if (it == ctx->windows.end()) {
+        std::unique_ptr<DeviceBuffer> b(new DeviceBuffer());
+        int st = b->ensure(sizeof(float) << logn, ctx->err);
+        if (st != GBFFT_OK) return fail(ctx, st, "%s", ctx->err.c_str());
+        GB_CUDA(ctx, hann_fill((float *)b->ptr, 1ull << logn, ctx->stream));
+        GB_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        it = ctx->windows.emplace(logn, std::move(b)).first;
+    }
+    *out = (const float *)it->second->ptr;
+    return GBFFT_OK;
+}
+
 // Enqueue one transform of the whole device batch on `stream` with variant v.
 int run_variant(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
                 const PlanVariant &v, cudaStream_t stream) {
     Plan *plan = nullptr;
     int st = get_plan(ctx, log2u(n), v, &plan);
     if (st != GBFFT_OK) return st;
+    const float *win = nullptr;
+    st = window_table(ctx, log2u(n), &win);
+    if (st != GBFFT_OK) return st;
     uint64_t launches = 0;
     std::string why;
-    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why);
+    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why, win);
     ctx->launches += launches;
     if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
                                     (unsigned long long)batch, why.c_str());
@@ -373,6 +399,14 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
     if (batch == 0) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "batch must be positive");
     GB_CUDA(ctx, cudaSetDevice(ctx->device));
     return autotune(ctx, n, batch, direction, best_seconds);
+}
+
+int gbfft_set_window(gbfft_ctx *ctx, int window) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (window != GBFFT_WINDOW_NONE && window != GBFFT_WINDOW_HANN)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "window %d is not provided", window);
+    ctx->window = window;
+    return GBFFT_OK;
 }
 
 int gbfft_set_precision(gbfft_ctx *ctx, int precision) {

@@ -27,6 +27,9 @@ struct TwiddleSegment {
     int logstride;
 };
 cudaError_t twiddle_fill(float2 *table, const TwiddleSegment *segs, int nseg, cudaStream_t stream);
+// Hann window table of n floats (FP64-computed).
+cudaError_t hann_fill(float *w, uint64_t n, cudaStream_t stream);
+constexpr int kWindowMaxLogN = 24;
 
 // ---- single-pass kernel (fft_rows.cu) ------------------------------------
 struct RowsKernelInfo {
@@ -44,6 +47,7 @@ bool rows_kernel_info(int logn, RowsKernelInfo &k);
 cudaError_t rows_prepare(RowsKernelInfo &k);
 // persistent: use fn_persistent with at most persist_ctas_per_sm * sms CTAs.
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
-                        const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream);
+                        const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
+                        const float *win = nullptr);
 
 }  // namespace gbfft

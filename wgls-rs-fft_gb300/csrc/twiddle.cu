@@ -60,4 +60,19 @@ cudaError_t twiddle_fill(float2 *table, const TwiddleSegment *segs, int nseg, cu
     return cudaGetLastError();
 }
 
+// Hann window w_i = 0.5 (1 - cos(2 pi i / (n - 1))) in FP64, rounded once to
+// f32 (the formula of the reference's host-side window, tests/test_utils.rs:
+// 39-48); n == 1 gives w_0 = 1.
+__global__ void hann_fill_kernel(float *w, uint64_t n) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    w[i] = n == 1 ? 1.0f : (float)(0.5 * (1.0 - cospi(2.0 * (double)i / (double)(n - 1))));
+}
+
+cudaError_t hann_fill(float *w, uint64_t n, cudaStream_t stream) {
+    const unsigned threads = 256;
+    hann_fill_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(w, n);
+    return cudaGetLastError();
+}
+
 }  // namespace gbfft

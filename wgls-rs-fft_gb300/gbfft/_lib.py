@@ -18,6 +18,8 @@ INVERSE = +1
 PREC_FP32 = 0
 PREC_TC_FP16 = 1
 PREC_TC_BF16X3 = 2
+WINDOW_NONE = 0
+WINDOW_HANN = 1
 
 OK = 0
 ERR_INVALID_SIZE = 1
@@ -53,6 +55,7 @@ SIGNATURES = {
     "gbfft_ragged_device": (_int, [_vp, _vp, _vp, _u64, _vp, ctypes.c_uint32, _vp]),
     "gbfft_bench_device": (_int, [_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_set_precision": (_int, [_vp, _int]),
+    "gbfft_set_window": (_int, [_vp, _int]),
     "gbfft_autotune": (_int, [_vp, _u64, _u64, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_launch_count": (_u64, [_vp]),
     "gbfft_version": (ctypes.c_char_p, []),
@@ -152,6 +155,10 @@ class Context:
 
     def set_precision(self, precision: int):
         self._check(self._L.gbfft_set_precision(self._h, precision))
+
+    def set_window(self, window: int):
+        """WINDOW_HANN: multiply every loaded input sample by the Hann window."""
+        self._check(self._L.gbfft_set_window(self._h, window))
 
     def c2c_host(self, x: np.ndarray, direction: int = FORWARD, out: np.ndarray | None = None) -> np.ndarray:
         """Transform a [batch, n] complex64 host array (contiguous); returns out."""

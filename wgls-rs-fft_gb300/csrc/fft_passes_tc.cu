@@ -45,14 +45,20 @@ struct PassTcCfg {
     static constexpr int THREADS = K::THREADS;
     static constexpr int NMMA = THREADS / 128;
     static constexpr uint32_t TMEM_COLS = NMMA * 32 <= 32 ? 32 : (NMMA * 32 <= 64 ? 64 : (NMMA * 32 <= 128 ? 128 : 256));
+    // The hi and lo A operands (THREADS rows x 64 bytes each) occupy exactly the
+    // bytes of the FP32 exchange tile (16 NG columns x R rows x 8 bytes): the
+    // tile is idle while a tensor-core DFT runs, so they share them.
     static constexpr size_t A_BYTES = (size_t)THREADS * kTcRowBytes;
+    static constexpr size_t TILE_BYTES = K::SMEM_ELEMS * sizeof(float2);  // exchange tile + column twiddles
+    static constexpr size_t OFF_TILE = 0;
     static constexpr size_t OFF_AHI = 0;
-    static constexpr size_t OFF_ALO = OFF_AHI + A_BYTES;
-    static constexpr size_t OFF_G = OFF_ALO + A_BYTES;                 // g_hi, g_lo (2 KB each)
-    static constexpr size_t OFF_TILE = OFF_G + 2 * kTcGBytes;          // FP32 exchange tile + column twiddles
-    static constexpr size_t OFF_MISC = OFF_TILE + K::SMEM_ELEMS * sizeof(float2);
+    static constexpr size_t OFF_ALO = A_BYTES;
+    static constexpr size_t OFF_G = TILE_BYTES;                 // g_hi, g_lo (2 KB each)
+    static constexpr size_t OFF_MISC = OFF_G + 2 * kTcGBytes;
     static constexpr size_t SMEM = OFF_MISC + 64;
-    static constexpr int MINB = THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 3);
+    static_assert(2 * A_BYTES <= (size_t)NG * kCols * (1 << LOGR) * sizeof(float2),
+                  "A operands must fit in the exchange tile (column twiddles follow it)");
+    static constexpr int MINB = THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 4);
 };
 
 template <int LOGR, bool FIRST, bool BF16>

@@ -165,7 +165,11 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
         ex = (int)((__float_as_uint(m) >> 23) & 0xff) - 127;
         ex = ex < -126 ? -126 : ex;
     }
-    const float down = __uint_as_float((uint32_t)(127 - ex) << 23);  // 2^-ex (ex in [-126, 127])
+    ex = ex > 126 ? 126 : ex;
+    const float down = __uint_as_float((uint32_t)(127 - ex) << 23);  // 2^-ex (ex in [-126, 126])
+    // A shares its bytes with the FP32 exchange tile: every thread must have
+    // finished reading its exchange inputs before any thread writes A.
+    __syncthreads();
     // 2. split into hi/lo rows of A
     uint32_t hi[16], lo[16];
 #pragma unroll

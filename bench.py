@@ -348,6 +348,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cufft", action="store_true", help="skip the reported cuFFT comparison")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -431,6 +432,24 @@ def main():
     ref64 = torch.fft.fft(xr, dim=1)
     acc = (torch.linalg.vector_norm(y[rows].to(torch.complex128) - ref64) / torch.linalg.vector_norm(ref64)).item()
 
+    # Reported GPU baseline: cuFFT (through torch.fft, batched C2C) on the same
+    # device batch, forward + inverse per step.  A library call, timed the same
+    # way; never part of this project's value.
+    cufft = None
+    if not args.no_cufft and args.window == "none":
+        for _ in range(3):
+            torch.fft.ifft(torch.fft.fft(x, dim=1), dim=1)
+        torch.cuda.synchronize(dev)
+        csteps = max(3, min(args.steps, 100))
+        ev0.record(stream)
+        for _ in range(csteps):
+            torch.fft.ifft(torch.fft.fft(x, dim=1), dim=1)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+        cms = ev0.elapsed_time(ev1)
+        cufft = {"value": samples_per_step * csteps / (cms * 1e-3) / 1e9, "unit": UNIT, "steps": csteps,
+                 "api": "torch.fft.fft/ifft (cuFFT), out of place"}
+
     # end to end through the host C ABI from pinned memory
     e2e = None
     if not args.no_e2e:
@@ -476,6 +495,7 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "launch_us": launch_s * 1e6},
             "cpu_baseline": cpu,
+            "cufft_baseline": cufft,
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": sampler.summary(),

@@ -191,6 +191,17 @@ int gbfft_set_precision(gbfft_ctx *ctx, int precision);
 #define GBFFT_WINDOW_HANN 1
 int gbfft_set_window(gbfft_ctx *ctx, int window);
 
+/* Gaussian noise added to every input sample as the transform loads it (fused:
+ * no extra pass), before the window: the reference pipeline's NOISE stage
+ * (examples/parallel_pipeline.rs:30-62).  Sample n of row b receives
+ * (r cos u2, r sin u2) with h1 = pcg(n * 1234567 + b * 7654321 + seed),
+ * h2 = pcg(h1 + 999983), u1 = max(h1 / 2^32, 1e-7), u2 = 2 pi h2 / 2^32,
+ * r = sigma sqrt(-2 ln u1) (the reference uses sigma = 0.1).  The hash is
+ * exact; log/sqrt/sin/cos are FP32 library functions.  sigma = 0 turns it off.
+ * With the Hann window on an inverse transform this gives the reference's
+ * noise -> FFT -> window -> IFFT -> scale pipeline in two launches. */
+int gbfft_set_noise(gbfft_ctx *ctx, uint32_t seed, float sigma);
+
 /* Autotuner (no reference counterpart; the reference's find_optimal_batch
  * example only sweeps batch sizes, examples/find_optimal_batch.rs:28).  Times
  * every plan variant for (n, batch, direction, current precision) -- global

@@ -217,6 +217,51 @@ def ref_fft_numpy(x, inverse: bool = False) -> np.ndarray:
 
 
 # ---------------------------------------------------------------------------
+# the reference's DSP pipeline stages (examples/parallel_pipeline.rs)
+# ---------------------------------------------------------------------------
+
+def _pcg_u32(v):
+    v = v.astype(np.uint32)
+    with np.errstate(over="ignore"):
+        s = v * np.uint32(747796405) + np.uint32(2891336453)
+        w = ((s >> ((s >> np.uint32(28)) + np.uint32(4))) ^ s) * np.uint32(277803737)
+    return (w >> np.uint32(22)) ^ w
+
+
+def ref_noise(batch: int, n: int, seed: int, sigma: float = 0.1) -> np.ndarray:
+    """NOISE stage (examples/parallel_pipeline.rs:36-62): for sample tid of row
+    batch_id, h1 = pcg(tid*1234567 + batch_id*7654321 + seed), h2 = pcg(h1 +
+    999983), u1 = max(f32(h1) * 2.328306437e-10, 1e-7), u2 = f32(h2) *
+    2.328306437e-10 * 6.283185307, r = sqrt(-2 ln u1) * sigma (0.1 there);
+    returns the [batch, n] complex64 noise (r cos u2, r sin u2), computed in
+    float32 like the shader."""
+    tid = np.arange(n, dtype=np.uint64)[None, :]
+    row = np.arange(batch, dtype=np.uint64)[:, None]
+    with np.errstate(over="ignore"):
+        v = ((tid * np.uint64(1234567) + row * np.uint64(7654321) + np.uint64(seed)) & np.uint64(0xFFFFFFFF))
+    h1 = _pcg_u32(v.astype(np.uint32))
+    with np.errstate(over="ignore"):
+        h2 = _pcg_u32(h1 + np.uint32(999983))
+    f = np.float32
+    u1 = np.maximum(h1.astype(f) * f(2.328306437e-10), f(1e-7))
+    u2 = h2.astype(f) * f(2.328306437e-10) * f(6.283185307)
+    r = np.sqrt(f(-2.0) * np.log(u1)) * f(sigma)
+    return (r * np.cos(u2) + 1j * (r * np.sin(u2))).astype(np.complex64)
+
+
+def ref_pipeline(x, seed: int, sigma: float = 0.1) -> np.ndarray:
+    """noise -> FFT -> Hann window over the bins -> IFFT (with 1/N) in FP64,
+    the reference's six-stage pipeline without its DMA stages."""
+    x = np.asarray(x)
+    b, n = x.shape
+    i = np.arange(n, dtype=np.float64)
+    w = np.ones(n) if n == 1 else 0.5 * (1.0 - np.cos(2.0 * np.pi * i / (n - 1)))
+    noisy = x.astype(np.complex128) + ref_noise(b, n, seed, sigma).astype(np.complex128)
+    spec = fft64(noisy)
+    return fft64(spec * w[None, :], inverse=True)
+
+
+# ---------------------------------------------------------------------------
 # metrics (src/benchmark.rs:272-297 and the relative-L2 gate)
 # ---------------------------------------------------------------------------
 

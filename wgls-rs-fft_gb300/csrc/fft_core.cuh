@@ -121,6 +121,35 @@ template <> struct Dft<16> {
     }
 };
 
+// Options applied to every sample as a transform loads it, in this order:
+//   x += noise (if sigma != 0), conjugate (inverse), x *= win[n] (if win).
+// The noise is the reference pipeline's NOISE stage
+// (larsjoost/wgls-rs-fft examples/parallel_pipeline.rs:36-62): PCG hash of
+// n * 1234567 + row * 7654321 + seed, Box-Muller with sigma (0.1 there).
+struct LoadOps {
+    const float *win;   // real window table of the transform length, or nullptr
+    uint32_t noise_seed;
+    float noise_sigma;  // 0 disables the noise
+    uint32_t row_base;  // batch index of the launch's first row (noise stream)
+};
+
+__host__ __device__ __forceinline__ uint32_t pcg_hash(uint32_t v) {
+    const uint32_t s = v * 747796405u + 2891336453u;
+    const uint32_t w = ((s >> ((s >> 28u) + 4u)) ^ s) * 277803737u;
+    return (w >> 22u) ^ w;
+}
+
+__device__ __forceinline__ float2 pipeline_noise(uint32_t n, uint32_t row, uint32_t seed, float sigma) {
+    const uint32_t h1 = pcg_hash(n * 1234567u + row * 7654321u + seed);
+    const uint32_t h2 = pcg_hash(h1 + 999983u);
+    const float u1 = fmaxf(__uint2float_rn(h1) * 2.328306437e-10f, 1e-7f);
+    const float u2 = __uint2float_rn(h2) * 2.328306437e-10f * 6.283185307f;
+    const float r = sqrtf(-2.0f * logf(u1)) * sigma;
+    float sn, cs;
+    sincosf(u2, &sn, &cs);
+    return make_float2(r * cs, r * sn);
+}
+
 // Streaming global access: every sample is read once and written once.
 __device__ __forceinline__ float2 ld_stream(const float2 *p) { return __ldcs(p); }
 __device__ __forceinline__ void st_stream(float2 *p, float2 v) { __stcs(p, v); }

@@ -39,7 +39,7 @@ template <int LOGR, bool FIRST>
 __global__ void __launch_bounds__(PassCfg<LOGR>::THREADS, PassCfg<LOGR>::MINB)
 fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                 const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
-                float in_im_sign, float out_re_scale, float out_im_scale, const float *__restrict__ win) {
+                float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
     extern __shared__ float2 smem_pass[];
     const int lognc = logn - LOGR;                     // log2 (columns per transform)
     const uint64_t tile = blockIdx.x;
@@ -58,7 +58,8 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
     a.out_re = out_re_scale;
     a.out_im = out_im_scale;
     a.coherent_load = false;
-    a.win = win;
+    a.row = (uint32_t)b;
+    a.ops = ops;
     pass_tile<LOGR, 1, FIRST>(a, smem_pass);
 }
 
@@ -69,7 +70,7 @@ template <int LOGR, bool FIRST>
 __global__ void __launch_bounds__(PassCfg<LOGR>::THREADS, PassCfg<LOGR>::MINB)
 fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                            const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
-                           float in_im_sign, float out_re_scale, float out_im_scale, const float *__restrict__ win,
+                           float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops,
                            uint64_t ntiles) {
     extern __shared__ float2 smem_pass[];
     constexpr int R = 1 << LOGR;
@@ -96,7 +97,8 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
         a.out_re = out_re_scale;
         a.out_im = out_im_scale;
         a.coherent_load = false;
-        a.win = win;
+        a.row = (uint32_t)b;
+        a.ops = ops;
         pass_tile<LOGR, 1, FIRST>(a, smem_pass);
         __syncthreads();  // shared memory is reused by the next tile
     }
@@ -146,7 +148,7 @@ cudaError_t pass_prepare(PassDesc &d) {
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                         float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
-                        bool persistent, int sms, const float *win) {
+                        bool persistent, int sms, LoadOps ops) {
     uint64_t tiles = batch << (logn - d.logr - kColsLog);
     if (tiles == 0) return cudaSuccess;
     int logp = d.logp;
@@ -154,14 +156,14 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
         const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)d.persist_ctas_per_sm * (uint64_t)sms);
         void *args[] = {(void *)&in,    (void *)&out,   (void *)&logn,     (void *)&logp,
                         (void *)&tw_sub, (void *)&tw_lo, (void *)&tw_hi,   (void *)&tw_split,
-                        (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale, (void *)&win,
+                        (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale, (void *)&ops,
                         (void *)&tiles};
         return cudaLaunchKernel(d.fn_persistent, dim3((unsigned)grid), dim3(d.threads), args, d.smem, stream);
     }
     if (tiles > 0x7fffffffull) return cudaErrorInvalidConfiguration;
     void *args[] = {(void *)&in,    (void *)&out,   (void *)&logn,     (void *)&logp,
                     (void *)&tw_sub, (void *)&tw_lo, (void *)&tw_hi,   (void *)&tw_split,
-                    (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale, (void *)&win};
+                    (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale, (void *)&ops};
     return cudaLaunchKernel(d.fn, dim3((unsigned)tiles), dim3(d.threads), args, d.smem, stream);
 }
 

@@ -66,7 +66,7 @@ __global__ void __launch_bounds__(PassTcCfg<LOGR>::THREADS, PassTcCfg<LOGR>::MIN
 fft_pass_tc_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                    const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                    float in_im_sign, float out_re_scale, float out_im_scale, const uint4 *__restrict__ gtab,
-                   uint32_t *err, const float *__restrict__ win) {
+                   uint32_t *err, LoadOps ops) {
     using C = PassTcCfg<LOGR>;
     extern __shared__ __align__(1024) uint8_t smem_tc[];
     uint64_t *bar = (uint64_t *)(smem_tc + C::OFF_MISC);
@@ -118,7 +118,8 @@ fft_pass_tc_kernel(const float2 *in, float2 *out, int logn, int logp, const floa
     a.out_re = out_re_scale;
     a.out_im = out_im_scale;
     a.coherent_load = false;
-    a.win = win;
+    a.row = (uint32_t)b;
+    a.ops = ops;
     pass_tile<LOGR, C::NG, FIRST>(a, (float2 *)(smem_tc + C::OFF_TILE), DftTc<BF16>{&st});
 
     tc_fence_before();
@@ -168,7 +169,7 @@ bool pass_tc_kernel_info(int logr, bool first, bool bf16, PassDesc &d) {
 cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                            const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, const void *gtab,
-                           uint32_t *err, cudaStream_t stream, const float *win) {
+                           uint32_t *err, cudaStream_t stream, LoadOps ops) {
     const uint64_t tiles = (batch << (logn - d.logr)) / (uint64_t)d.cols;
     if (tiles == 0) return cudaSuccess;
     if (tiles > 0x7fffffffull) return cudaErrorInvalidConfiguration;
@@ -176,7 +177,7 @@ cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uin
     void *args[] = {(void *)&in,     (void *)&out,   (void *)&logn,      (void *)&logp,
                     (void *)&tw_sub, (void *)&tw_lo, (void *)&tw_hi,     (void *)&tw_split,
                     (void *)&in_im_sign, (void *)&out_re_scale, (void *)&out_im_scale, (void *)&gtab,
-                    (void *)&err, (void *)&win};
+                    (void *)&err, (void *)&ops};
     return cudaLaunchKernel(d.fn, dim3((unsigned)tiles), dim3(d.threads), args, d.smem, stream);
 }
 

@@ -87,9 +87,9 @@ __device__ __forceinline__ void rag_rows(const RagParams &P, const RagItem &it, 
         const RagXform x = P.xf[P.order[it.a + (act ? g : 0)]];
         const bool inv = x.dir == GBFFT_INVERSE;
         const float sc = inv ? ldexpf(1.0f, -L) : 1.0f;
-        return RowRef{P.in + x.offset, P.out + x.offset, act, inv ? -1.0f : 1.0f, sc, inv ? -sc : 1.0f, nullptr};
+        return RowRef{P.in + x.offset, P.out + x.offset, act, inv ? -1.0f : 1.0f, sc, inv ? -sc : 1.0f, 0u};
     };
-    rows_tile<L, G>(ref, P.sub[L], smem);
+    rows_tile<L, G>(ref, P.sub[L], smem, LoadOps{nullptr, 0u, 0.f, 0u});
 }
 
 // Returns false when the wait for the first pass gave up.
@@ -132,7 +132,8 @@ __device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, 
     a.out_re = FIRST ? 1.0f : sc;
     a.out_im = FIRST ? 1.0f : (inv ? -sc : 1.0f);
     a.coherent_load = !FIRST;
-    a.win = nullptr;
+    a.row = 0;
+    a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
     pass_tile<LOGR, NG, FIRST>(a, smem);
     if (FIRST) {
         __threadfence();  // this thread's workspace stores are visible GPU-wide

@@ -37,14 +37,15 @@ struct RowsCfg : SubCfg<LOGN> {
 template <int LOGN>
 __global__ void __launch_bounds__(RowsCfg<LOGN>::THREADS, RowsCfg<LOGN>::MINB)
 fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
-                float in_im_sign, float out_re_scale, float out_im_scale, const float *__restrict__ win) {
+                float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
     using C = RowsCfg<LOGN>;
     extern __shared__ float2 smem_rows[];
     auto ref = [&](int g) {
         const uint64_t row = (uint64_t)blockIdx.x * C::G + g;
-        return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale, win};
+        return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
+                      (uint32_t)row};
     };
-    rows_tile<LOGN, C::G>(ref, tw, smem_rows);
+    rows_tile<LOGN, C::G>(ref, tw, smem_rows, ops);
 }
 
 // Persistent variant for the sizes whose per-transform footprint allows only
@@ -55,8 +56,7 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
 template <int LOGN>
 __global__ void __launch_bounds__(RowsCfg<LOGN>::THREADS, RowsCfg<LOGN>::MINB)
 fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
-                           float in_im_sign, float out_re_scale, float out_im_scale,
-                           const float *__restrict__ win) {
+                           float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
     using C = RowsCfg<LOGN>;
     extern __shared__ float2 smem_rows[];
     constexpr uint32_t kTileSamples = C::G * C::N;
@@ -71,9 +71,10 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
         }
         auto ref = [&](int g) {
             const uint64_t row = tile * C::G + g;
-            return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale, win};
+            return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
+                      (uint32_t)row};
         };
-        rows_tile<LOGN, C::G>(ref, tw, smem_rows);
+        rows_tile<LOGN, C::G>(ref, tw, smem_rows, ops);
         __syncthreads();  // shared memory is reused by the next tile
     }
 }
@@ -120,7 +121,7 @@ cudaError_t rows_prepare(RowsKernelInfo &k) {
 
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
                         const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
-                        const float *win) {
+                        LoadOps ops) {
     if (batch == 0) return cudaSuccess;
     uint64_t ctas = (batch + k.transforms_per_cta - 1) / k.transforms_per_cta;
     const void *fn = k.fn;
@@ -134,7 +135,7 @@ cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, 
     float in_im = inv ? -1.0f : 1.0f;
     float out_re = scale, out_im = inv ? -scale : 1.0f;
     void *args[] = {(void *)&in, (void *)&out, (void *)&batch, (void *)&tw,
-                    (void *)&in_im, (void *)&out_re, (void *)&out_im, (void *)&win};
+                    (void *)&in_im, (void *)&out_re, (void *)&out_im, (void *)&ops};
     return cudaLaunchKernel(fn, dim3((unsigned)ctas), dim3(k.threads), args, k.smem, stream);
 }
 

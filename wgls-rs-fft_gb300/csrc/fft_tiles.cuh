@@ -53,13 +53,14 @@ struct RowRef {
     float2 *dst;
     bool active;
     float in_im, out_re, out_im;
-    const float *win;  // window multiplied into each loaded sample, or nullptr
+    uint32_t row;      // batch index (noise stream)
 };
 
 // G transforms of length 2^LOGN; thread tid = g*T + t.  `ref(g)` gives the
 // transform's RowRef.  smem holds G*N complex values (unused if NSUB == 1).
 template <int LOGN, int G, class RefFn, class Eng = DftRegs>
-__device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem, Eng eng = Eng()) {
+__device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem, const LoadOps &ops,
+                                          Eng eng = Eng()) {
     using C = SubCfg<LOGN>;
     const int tid = threadIdx.x;
     const int g = tid >> C::LOGT;
@@ -69,13 +70,17 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
 #pragma unroll
     for (int e = 0; e < C::E; ++e) {
         float2 x = r.active ? ld_stream(r.src + t + C::T * e) : make_float2(0.f, 0.f);
+        if (ops.noise_sigma != 0.f) {
+            const float2 z = pipeline_noise(t + C::T * e, ops.row_base + r.row, ops.noise_seed, ops.noise_sigma);
+            x = make_float2(x.x + z.x, x.y + z.y);
+        }
         x.y *= r.in_im;
         v[e] = x;
     }
-    if (r.win != nullptr) {
+    if (ops.win != nullptr) {
 #pragma unroll
         for (int e = 0; e < C::E; ++e) {
-            const float w = __ldg(r.win + t + C::T * e);
+            const float w = __ldg(ops.win + t + C::T * e);
             v[e] = make_float2(v[e].x * w, v[e].y * w);
         }
     }
@@ -147,7 +152,8 @@ struct PassArgs {
     int tw_split;
     float in_im, out_re, out_im;
     bool coherent_load;  // input written earlier in the same kernel: bypass L1
-    const float *win;    // first pass: window multiplied into each loaded sample, or nullptr
+    uint32_t row;        // batch index of the transform (noise stream)
+    LoadOps ops;         // first pass: noise / window applied on load
 };
 
 // NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
@@ -173,13 +179,18 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
         const uint32_t m = t + T * e;
         const float2 *p = a.src + j + ((uint64_t)m << lognc);
         float2 x = a.coherent_load ? __ldcg(p) : ld_stream(p);
+        if (FIRST && a.ops.noise_sigma != 0.f) {
+            const float2 z = pipeline_noise(j + (m << lognc), a.ops.row_base + a.row, a.ops.noise_seed,
+                                           a.ops.noise_sigma);
+            x = make_float2(x.x + z.x, x.y + z.y);
+        }
         x.y *= a.in_im;
         v[e] = x;
     }
-    if (FIRST && a.win != nullptr) {
+    if (FIRST && a.ops.win != nullptr) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
-            const float w = __ldg(a.win + j + ((uint64_t)(t + T * e) << lognc));
+            const float w = __ldg(a.ops.win + j + ((uint64_t)(t + T * e) << lognc));
             v[e] = make_float2(v[e].x * w, v[e].y * w);
         }
     }

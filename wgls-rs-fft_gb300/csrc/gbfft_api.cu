@@ -38,6 +38,8 @@ struct gbfft_ctx {
     std::map<std::tuple<int, int, PlanVariant>, std::unique_ptr<Plan>> plans;
     std::map<std::tuple<int, int, int, int>, PlanVariant> tuned;
     int window = GBFFT_WINDOW_NONE;
+    uint32_t noise_seed = 0;
+    float noise_sigma = 0.f;  // 0: no noise added on load
     std::map<int, std::unique_ptr<DeviceBuffer>> windows;  // Hann tables by log2 N
     bool auto_tune = false;
     bool tune_verbose = false;  // GBFFT_AUTOTUNE_VERBOSE=1: per-variant timings on stderr
@@ -209,7 +211,7 @@ int window_table(gbfft_ctx *ctx, int logn, const float **out) {
 
 // Enqueue one transform of the whole device batch on `stream` with variant v.
 int run_variant(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
-                const PlanVariant &v, cudaStream_t stream) {
+                const PlanVariant &v, cudaStream_t stream, uint64_t row_base = 0) {
     Plan *plan = nullptr;
     int st = get_plan(ctx, log2u(n), v, &plan);
     if (st != GBFFT_OK) return st;
@@ -218,7 +220,8 @@ int run_variant(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint6
     if (st != GBFFT_OK) return st;
     uint64_t launches = 0;
     std::string why;
-    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why, win);
+    const LoadOps ops{win, ctx->noise_seed, ctx->noise_sigma, (uint32_t)row_base};
+    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why, ops);
     ctx->launches += launches;
     if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
                                     (unsigned long long)batch, why.c_str());
@@ -300,12 +303,14 @@ void load_tune_cache(gbfft_ctx *ctx) {
 }
 
 // Enqueue one transform of the whole device batch on `stream`.
+// row_base: batch index of in[0] within the caller's batch (keeps the fused
+// noise stream continuous when a host batch is processed in chunks).
 int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64_t batch, int direction,
-               cudaStream_t stream) {
+               cudaStream_t stream, uint64_t row_base = 0) {
     int st = GBFFT_OK;
     const PlanVariant v = choose_variant(ctx, log2u(n), batch, direction, st);
     if (st != GBFFT_OK) return st;
-    return run_variant(ctx, in, out, n, batch, direction, v, stream);
+    return run_variant(ctx, in, out, n, batch, direction, v, stream, row_base);
 }
 
 }  // namespace
@@ -409,6 +414,15 @@ int gbfft_set_window(gbfft_ctx *ctx, int window) {
     return GBFFT_OK;
 }
 
+int gbfft_set_noise(gbfft_ctx *ctx, uint32_t seed, float sigma) {
+    if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
+    if (!(sigma >= 0.f) || sigma == INFINITY)
+        return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "noise sigma must be finite and >= 0");
+    ctx->noise_seed = seed;
+    ctx->noise_sigma = sigma;
+    return GBFFT_OK;
+}
+
 int gbfft_set_precision(gbfft_ctx *ctx, int precision) {
     if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
     if (precision != GBFFT_PREC_FP32 && precision != GBFFT_PREC_TC_FP16 && precision != GBFFT_PREC_TC_BF16X3)
@@ -459,7 +473,8 @@ static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t
         const size_t len = (size_t)rows * row_bytes;
         cudaStream_t s = ctx->xfer[k % 3];
         GB_CUDA(ctx, cudaMemcpyAsync((char *)d + off, (const char *)src + off, len, cudaMemcpyHostToDevice, s));
-        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)d + off), n, rows, direction, s);
+        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)d + off), n, rows, direction, s,
+                        done);
         if (st != GBFFT_OK) return st;
         GB_CUDA(ctx, cudaMemcpyAsync((char *)dst + off, (char *)d + off, len, cudaMemcpyDeviceToHost, s));
         done += rows;

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include "../../include/gbfft.h"
+#include "fft_core.cuh"
 
 namespace gbfft {
 
@@ -48,6 +49,6 @@ cudaError_t rows_prepare(RowsKernelInfo &k);
 // persistent: use fn_persistent with at most persist_ctas_per_sm * sms CTAs.
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
                         const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
-                        const float *win = nullptr);
+                        LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 
 }  // namespace gbfft

@@ -159,12 +159,12 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
 }
 
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction, DeviceBuffer &ws,
-                 uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why, const float *win) {
+                 uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why, LoadOps ops) {
     launches = 0;
     if (batch == 0) return GBFFT_OK;
     cudaError_t e;
     if (!p.multipass) {
-        e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.variant.persistent, p.sms, stream, win);
+        e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.variant.persistent, p.sms, stream, ops);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;
@@ -208,11 +208,11 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
         if (d.tc)
             e = pass_tc_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
                                p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, p.gtab, err, stream,
-                               i == 0 ? win : nullptr);
+                               i == 0 ? ops : LoadOps{nullptr, 0u, 0.f, 0u});
         else
             e = pass_launch(d, src[i], dst[i], batch, p.logn, p.tw + d.sub_tw_offset, p.tw + p.tw_lo_offset,
                             p.tw + p.tw_hi_offset, p.tw_split, in_im, out_re, out_im, stream, p.variant.persistent,
-                            p.sms, i == 0 ? win : nullptr);
+                            p.sms, i == 0 ? ops : LoadOps{nullptr, 0u, 0.f, 0u});
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;

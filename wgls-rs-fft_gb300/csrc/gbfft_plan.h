@@ -72,14 +72,14 @@ cudaError_t pass_prepare(PassDesc &d);
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                         float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
-                        bool persistent = false, int sms = 0, const float *win = nullptr);
+                        bool persistent = false, int sms = 0, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 
 // fft_passes_tc.cu (split-precision tensor-core form)
 bool pass_tc_kernel_info(int logr, bool first, bool bf16, PassDesc &d);
 cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                            const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, const void *gtab,
-                           uint32_t *err, cudaStream_t stream, const float *win = nullptr);
+                           uint32_t *err, cudaStream_t stream, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
 constexpr size_t kTcGtabBytes = 4 * 2048;
 
@@ -100,9 +100,9 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision);
 
 int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStream_t stream, std::string &why);
 // `err` is a device flag the tensor-core kernels raise when a bounded wait gives up.
-// `win`: window multiplied into every loaded input sample (nullptr = none).
+// `ops`: noise / window applied to every loaded input sample.
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,
                  DeviceBuffer &ws, uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why,
-                 const float *win = nullptr);
+                 LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 
 }  // namespace gbfft

@@ -56,6 +56,7 @@ SIGNATURES = {
     "gbfft_bench_device": (_int, [_vp, _u64, _u64, _int, _int, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_set_precision": (_int, [_vp, _int]),
     "gbfft_set_window": (_int, [_vp, _int]),
+    "gbfft_set_noise": (_int, [_vp, ctypes.c_uint32, ctypes.c_float]),
     "gbfft_autotune": (_int, [_vp, _u64, _u64, _int, ctypes.POINTER(ctypes.c_double)]),
     "gbfft_launch_count": (_u64, [_vp]),
     "gbfft_version": (ctypes.c_char_p, []),
@@ -159,6 +160,10 @@ class Context:
     def set_window(self, window: int):
         """WINDOW_HANN: multiply every loaded input sample by the Hann window."""
         self._check(self._L.gbfft_set_window(self._h, window))
+
+    def set_noise(self, seed: int, sigma: float):
+        """Add the reference pipeline's PCG/Box-Muller noise on load (sigma 0: off)."""
+        self._check(self._L.gbfft_set_noise(self._h, seed, sigma))
 
     def c2c_host(self, x: np.ndarray, direction: int = FORWARD, out: np.ndarray | None = None) -> np.ndarray:
         """Transform a [batch, n] complex64 host array (contiguous); returns out."""

@@ -423,14 +423,14 @@ def main():
     # check the last step's roundtrip (cheap, catches a broken build), and the
     # forward result of a few rows against a float64 FFT of the same rows
     rt = (torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x)).item()
-    rows = sorted({0, batch // 2, batch - 1})
-    xr = x[rows].to(torch.complex128)
+    acc_rows = sorted({0, batch // 2, batch - 1})
+    xr = x[acc_rows].to(torch.complex128)
     if args.window == "hann":  # the fused window multiplies every loaded sample
         from gbfft import signals
         xr = xr * torch.from_numpy(signals.hann_window(n).astype("float64")).to(dev)[None, :]
         rt = None              # both directions load through the window: no roundtrip identity
     ref64 = torch.fft.fft(xr, dim=1)
-    acc = (torch.linalg.vector_norm(y[rows].to(torch.complex128) - ref64) / torch.linalg.vector_norm(ref64)).item()
+    acc = (torch.linalg.vector_norm(y[acc_rows].to(torch.complex128) - ref64) / torch.linalg.vector_norm(ref64)).item()
 
     # Reported GPU baseline: cuFFT (through torch.fft, batched C2C) on the same
     # device batch, forward + inverse per step.  A library call, timed the same
@@ -500,7 +500,7 @@ def main():
             "gpu_launches": launches,
             "clocks": sampler.summary(),
             "roundtrip_rel_l2": rt,
-            "accuracy": {"precision": args.precision, "rel_l2_vs_fp64": acc, "rows": rows,
+            "accuracy": {"precision": args.precision, "rel_l2_vs_fp64": acc, "rows": acc_rows,
                          "reference": "float64 torch.fft of the sampled rows (checker only)"},
         }
         print(json.dumps(line), flush=True)

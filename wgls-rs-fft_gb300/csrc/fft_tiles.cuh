@@ -67,16 +67,19 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
     const int t = tid & (C::T - 1);
     const RowRef r = ref(g);
     float2 v[C::E];
+    // All E loads first, back to back (the branch on the noise stays outside
+    // the load loop so nothing serialises them).
 #pragma unroll
-    for (int e = 0; e < C::E; ++e) {
-        float2 x = r.active ? ld_stream(r.src + t + C::T * e) : make_float2(0.f, 0.f);
-        if (ops.noise_sigma != 0.f) {
+    for (int e = 0; e < C::E; ++e) v[e] = r.active ? ld_stream(r.src + t + C::T * e) : make_float2(0.f, 0.f);
+    if (ops.noise_sigma != 0.f) {
+#pragma unroll
+        for (int e = 0; e < C::E; ++e) {
             const float2 z = pipeline_noise(t + C::T * e, ops.row_base + r.row, ops.noise_seed, ops.noise_sigma);
-            x = make_float2(x.x + z.x, x.y + z.y);
+            v[e] = make_float2(v[e].x + z.x, v[e].y + z.y);
         }
-        x.y *= r.in_im;
-        v[e] = x;
     }
+#pragma unroll
+    for (int e = 0; e < C::E; ++e) v[e].y *= r.in_im;
     if (ops.win != nullptr) {
 #pragma unroll
         for (int e = 0; e < C::E; ++e) {
@@ -174,19 +177,24 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
     const uint32_t j = j0 + c;
 
     float2 v[E];
+    // All E loads first, back to back; options are applied afterwards.
+    if (a.coherent_load) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-        const uint32_t m = t + T * e;
-        const float2 *p = a.src + j + ((uint64_t)m << lognc);
-        float2 x = a.coherent_load ? __ldcg(p) : ld_stream(p);
-        if (FIRST && a.ops.noise_sigma != 0.f) {
-            const float2 z = pipeline_noise(j + (m << lognc), a.ops.row_base + a.row, a.ops.noise_seed,
-                                           a.ops.noise_sigma);
-            x = make_float2(x.x + z.x, x.y + z.y);
-        }
-        x.y *= a.in_im;
-        v[e] = x;
+        for (int e = 0; e < E; ++e) v[e] = __ldcg(a.src + j + ((uint64_t)(t + T * e) << lognc));
+    } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = ld_stream(a.src + j + ((uint64_t)(t + T * e) << lognc));
     }
+    if (FIRST && a.ops.noise_sigma != 0.f) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+            const float2 z = pipeline_noise(j + ((uint32_t)(t + T * e) << lognc), a.ops.row_base + a.row,
+                                           a.ops.noise_seed, a.ops.noise_sigma);
+            v[e] = make_float2(v[e].x + z.x, v[e].y + z.y);
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e].y *= a.in_im;
     if (FIRST && a.ops.win != nullptr) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {

@@ -17,7 +17,7 @@ TOL_REL_L2 = 2e-6
 def _cache_line(logn, batch, direction, max_logr, persistent, precision=0):
     return json.dumps({"arch": "sm_103", "logn": logn, "precision": precision, "direction": direction,
                        "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": persistent,
-                       "seconds": 1.0})
+                       "fused": 0, "seconds": 1.0})
 
 
 @pytest.mark.parametrize("logn,batch,max_logr,persistent", [

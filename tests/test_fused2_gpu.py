@@ -1,0 +1,119 @@
+"""GPU: the fused two-pass form (both global passes of N = 2^15 .. 2^20 in one
+persistent launch, intermediate read back from L2).
+
+The form runs the same tile arithmetic as the two-launch form, so its output
+must be bit-identical to it; both are also checked against FP64 at
+rel-L2 <= 2e-6.  Variants are forced through the on-disk tuning cache
+(GBFFT_AUTOTUNE_CACHE).  Covered: batches smaller than, equal to and far
+larger than the producer/consumer lag, both directions, repeated launches
+(the kernel clears its own counters), two streams, noise on load, and the
+in-place fallback."""
+import json
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_REL_L2 = 2e-6
+
+
+@pytest.fixture(scope="module")
+def torch():
+    t = pytest.importorskip("torch")
+    assert t.cuda.is_available()
+    return t
+
+
+def _force(tmp_path, monkeypatch, logn, batch, fused, max_logr=10):
+    import gbfft
+    lines = []
+    for d in (gbfft.FORWARD, gbfft.INVERSE):
+        lines.append(json.dumps({"arch": "sm_103", "logn": logn, "precision": 0, "direction": d,
+                                 "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": 0,
+                                 "fused": int(fused), "seconds": 1.0}))
+    cache = tmp_path / f"tune_{int(fused)}.jsonl"
+    cache.write_text("\n".join(lines) + "\n")
+    monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+
+
+def _run(torch, x, direction, fused, tmp_path, monkeypatch, repeats=1, noise=None):
+    import gbfft
+    batch, n = x.shape
+    _force(tmp_path, monkeypatch, n.bit_length() - 1, batch, fused)
+    dx = torch.from_numpy(x).cuda()
+    outs = []
+    with gbfft.Context(0) as ctx:
+        if noise:
+            ctx.set_noise(*noise)
+        for _ in range(repeats):
+            dy = torch.full_like(dx, float("nan"))
+            ctx.c2c_device(dx, dy, n, batch, direction)
+            torch.cuda.synchronize()
+            outs.append(dy.cpu().numpy())
+        launches = ctx.launch_count()
+    return outs, launches
+
+
+@pytest.mark.parametrize("logn,batch", [(15, 1), (15, 37), (16, 3), (16, 200), (17, 5), (18, 9), (19, 2), (20, 3)])
+def test_fused_matches_two_launches_and_fp64(torch, oracle, lib_built, tmp_path, monkeypatch, logn, batch):
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=300 + logn)
+    for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        (yf,), lf = _run(torch, x, d, True, tmp_path, monkeypatch)
+        (yp,), lp = _run(torch, x, d, False, tmp_path, monkeypatch)
+        assert lf == 1 and lp == 2  # one launch against two
+        assert np.array_equal(yf, yp)
+        assert oracle.rel_l2(yf, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2
+
+
+def test_fused_repeated_launches_reset_counters(torch, lib_built, tmp_path, monkeypatch):
+    import gbfft
+    from gbfft import signals
+    x = signals.uniform_c64(96, 1 << 16, seed=310)
+    outs, launches = _run(torch, x, gbfft.FORWARD, True, tmp_path, monkeypatch, repeats=5)
+    assert launches == 5
+    for y in outs[1:]:
+        assert np.array_equal(y, outs[0])
+
+
+def test_fused_two_streams(torch, oracle, lib_built, tmp_path, monkeypatch):
+    import gbfft
+    from gbfft import signals
+    n, batch = 1 << 17, 24
+    _force(tmp_path, monkeypatch, 17, batch, True)
+    xs = [signals.normal_c64(batch, n, seed=320 + i) for i in range(2)]
+    dxs = [torch.from_numpy(x).cuda() for x in xs]
+    dys = [torch.empty_like(d) for d in dxs]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    torch.cuda.synchronize()
+    with gbfft.Context(0) as ctx:
+        for rep in range(3):
+            for i in range(2):
+                ctx.c2c_device(dxs[i], dys[i], n, batch, gbfft.FORWARD, stream=streams[i].cuda_stream)
+        torch.cuda.synchronize()
+    for i in range(2):
+        assert oracle.rel_l2(dys[i].cpu().numpy(), oracle.fft64(xs[i])) <= TOL_REL_L2
+
+
+def test_fused_noise_on_load(torch, lib_built, tmp_path, monkeypatch):
+    import gbfft
+    x = np.zeros((12, 1 << 15), np.complex64)
+    (yf,), _ = _run(torch, x, gbfft.FORWARD, True, tmp_path, monkeypatch, noise=(9, 0.5))
+    (yp,), _ = _run(torch, x, gbfft.FORWARD, False, tmp_path, monkeypatch, noise=(9, 0.5))
+    assert np.array_equal(yf, yp) and np.abs(yf).max() > 0
+
+
+def test_fused_in_place_falls_back(torch, oracle, lib_built, tmp_path, monkeypatch):
+    import gbfft
+    from gbfft import signals
+    n, batch = 1 << 16, 7
+    _force(tmp_path, monkeypatch, 16, batch, True)
+    x = signals.normal_c64(batch, n, seed=330)
+    d = torch.from_numpy(x).cuda()
+    with gbfft.Context(0) as ctx:
+        ctx.c2c_device(d, d, n, batch, gbfft.INVERSE)
+        torch.cuda.synchronize()
+        assert ctx.launch_count() == 2
+    assert oracle.rel_l2(d.cpu().numpy(), oracle.fft64(x, inverse=True)) <= TOL_REL_L2

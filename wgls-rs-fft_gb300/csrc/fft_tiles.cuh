@@ -153,8 +153,10 @@ struct PassArgs {
     uint32_t col0;      // first column of the tile (multiple of NG*16)
     const float2 *tw_sub, *tw_lo, *tw_hi;
     int tw_split;
-    float in_im, out_re, out_im;
+    float in_im;          // -1: conjugate the input (first pass of an inverse)
+    float out_re, out_im; // output scale; later passes only (a first pass never scales)
     bool coherent_load;  // input written earlier in the same kernel: bypass L1
+    bool keep_l2 = false;  // first pass: output is read again soon, store it with normal L2 priority
     uint32_t row;        // batch index of the transform (noise stream)
     LoadOps ops;         // first pass: noise / window applied on load
 };
@@ -193,8 +195,10 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
             v[e] = make_float2(v[e].x + z.x, v[e].y + z.y);
         }
     }
+    if (a.in_im != 1.0f) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e].y *= a.in_im;
+        for (int e = 0; e < E; ++e) v[e].y *= a.in_im;
+    }
     if (FIRST && a.ops.win != nullptr) {
 #pragma unroll
         for (int e = 0; e < E; ++e) {
@@ -236,23 +240,34 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
             }
         __syncthreads();
         float2 *blk = a.dst + (uint64_t)j0 * R;
+        if (a.keep_l2) {
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-            const int lin = lt + kCols * T * e;
-            const int cc = lin >> LOGR, q = lin & (R - 1);
-            const float2 y = buf[cc * R + (q ^ cc)];
-            st_stream(blk + lin, make_float2(y.x * a.out_re, y.y * a.out_im));
+            for (int e = 0; e < E; ++e) {
+                const int lin = lt + kCols * T * e;
+                const int cc = lin >> LOGR, q = lin & (R - 1);
+                __stcg(blk + lin, buf[cc * R + (q ^ cc)]);
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < E; ++e) {
+                const int lin = lt + kCols * T * e;
+                const int cc = lin >> LOGR, q = lin & (R - 1);
+                st_stream(blk + lin, buf[cc * R + (q ^ cc)]);
+            }
         }
     } else {
         const uint32_t pmask = (1u << a.logp) - 1;
         float2 *col = a.dst + ((uint64_t)(j >> a.logp) << (LOGR + a.logp)) + (j & pmask);
+        if (a.out_re != 1.0f || a.out_im != 1.0f) {
+#pragma unroll
+            for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.out_re, v[e].y * a.out_im);
+        }
 #pragma unroll
         for (int bb = 0; bb < NB; ++bb)
 #pragma unroll
             for (int q = 0; q < (1 << LR); ++q) {
                 const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
-                const float2 y = v[bb + q * NB];
-                st_stream(col + ((uint64_t)pos << a.logp), make_float2(y.x * a.out_re, y.y * a.out_im));
+                st_stream(col + ((uint64_t)pos << a.logp), v[bb + q * NB]);
             }
     }
 }

@@ -47,6 +47,9 @@ struct gbfft_ctx {
     DeviceBuffer tune_a, tune_b;  // scratch for the autotuner
     DeviceBuffer dbuf;    // device copy of a host batch
     DeviceBuffer ws;      // multi-pass workspace
+    // counter blocks of the fused two-pass form, one per stream so that calls
+    // on different streams never share one
+    std::map<cudaStream_t, std::unique_ptr<DeviceBuffer>> fused_ctr;
     uint32_t *d_err = nullptr;  // raised by tensor-core kernels when a bounded wait gives up
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
@@ -221,7 +224,13 @@ int run_variant(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint6
     uint64_t launches = 0;
     std::string why;
     const LoadOps ops{win, ctx->noise_seed, ctx->noise_sigma, (uint32_t)row_base};
-    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why, ops);
+    DeviceBuffer *ctr = nullptr;
+    if (plan->has_fused) {
+        std::unique_ptr<DeviceBuffer> &b = ctx->fused_ctr[stream];
+        if (!b) b.reset(new DeviceBuffer());
+        ctr = b.get();
+    }
+    st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why, ops, ctr);
     ctx->launches += launches;
     if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
                                     (unsigned long long)batch, why.c_str());
@@ -260,8 +269,10 @@ int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *
         GB_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
         const double s = (double)ms * 1e-3 / reps;
         if (ctx->tune_verbose)
-            fprintf(stderr, "gbfft autotune N=2^%d batch=%llu dir=%d prec=%d max_logr=%d persistent=%d: %.3f us\n",
+            fprintf(stderr,
+                    "gbfft autotune N=2^%d batch=%llu dir=%d prec=%d max_logr=%d persistent=%d fused=%d: %.3f us\n",
                     logn, (unsigned long long)batch, direction, ctx->precision, v.max_logr, v.persistent ? 1 : 0,
+                    v.fused ? 1 : 0,
                     s * 1e6);
         if (s < best) {
             best = s;
@@ -277,8 +288,9 @@ int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *
         if (f) {
             fprintf(f,
                     "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
-                    "\"max_logr\": %d, \"persistent\": %d, \"seconds\": %.9g}\n",
+                    "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"seconds\": %.9g}\n",
                     logn, ctx->precision, direction, log2floor(batch), best_v.max_logr, best_v.persistent ? 1 : 0,
+                    best_v.fused ? 1 : 0,
                     best);
             fclose(f);
         }
@@ -291,13 +303,13 @@ void load_tune_cache(gbfft_ctx *ctx) {
     if (!f) return;
     char line[512];
     while (fgets(line, sizeof line, f)) {
-        int logn, prec, dir, blog, mlr, pers;
+        int logn, prec, dir, blog, mlr, pers, fused;
         double sec;
         if (sscanf(line,
                    "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
-                   "\"max_logr\": %d, \"persistent\": %d, \"seconds\": %lf}",
-                   &logn, &prec, &dir, &blog, &mlr, &pers, &sec) == 7)
-            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] = PlanVariant{mlr, pers != 0};
+                   "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"seconds\": %lf}",
+                   &logn, &prec, &dir, &blog, &mlr, &pers, &fused, &sec) == 8)
+            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] = PlanVariant{mlr, pers != 0, fused != 0};
     }
     fclose(f);
 }

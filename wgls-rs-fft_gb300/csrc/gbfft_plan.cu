@@ -78,6 +78,9 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         bool dup = false;
         for (const PlanVariant &v : c) dup |= split_passes(logn, v.max_logr) == parts;
         if (dup || parts[0] < 5) continue;
+        Fused2Desc fd;
+        if (!tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd))
+            c.push_back(PlanVariant{m, false, true});
         c.push_back(PlanVariant{m, false});
         if (!tc) c.push_back(PlanVariant{m, true});
     }
@@ -132,6 +135,13 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
             p.passes.push_back(d);
         }
         p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
+        if (v.fused && !tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], p.fused)) {
+            if ((e = fused2_prepare(p.fused)) != cudaSuccess) {
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_CUDA;
+            }
+            p.has_fused = p.fused.ctas_per_sm > 0;
+        }
         if (tc) {
             if ((e = cudaMalloc(&p.gtab, kTcGtabBytes)) != cudaSuccess) {
                 cudaGetLastError();
@@ -159,10 +169,35 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
 }
 
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction, DeviceBuffer &ws,
-                 uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why, LoadOps ops) {
+                 uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why, LoadOps ops,
+                 DeviceBuffer *ctr) {
     launches = 0;
     if (batch == 0) return GBFFT_OK;
     cudaError_t e;
+    if (p.has_fused && ctr && (const void *)in != (const void *)out && batch <= 0x7fffffffull) {
+        const size_t want = (2 + (size_t)batch) * sizeof(uint32_t);
+        if (ctr->bytes < want) {
+            int st = ctr->ensure(want, why);
+            if (st != GBFFT_OK) return st;
+            // the kernel leaves the block zeroed; a new block starts zeroed
+            if ((e = cudaMemsetAsync(ctr->ptr, 0, ctr->bytes, stream)) != cudaSuccess) {
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_CUDA;
+            }
+        }
+        const bool inv = direction == GBFFT_INVERSE;
+        const float scale = inv ? ldexpf(1.0f, -p.logn) : 1.0f;
+        const PassDesc &d1 = p.passes[0], &d2 = p.passes[1];
+        e = fused2_launch(p.fused, in, out, batch, p.logn, p.tw + d1.sub_tw_offset, p.tw + d2.sub_tw_offset,
+                          p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset, p.tw_split, inv ? -1.0f : 1.0f, scale,
+                          inv ? -scale : 1.0f, ops, (uint32_t *)ctr->ptr, err, p.sms, stream);
+        if (e != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        launches = 1;
+        return GBFFT_OK;
+    }
     if (!p.multipass) {
         e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.variant.persistent, p.sms, stream, ops);
         if (e != cudaSuccess) {

@@ -36,15 +36,35 @@ struct PassDesc {
     bool tc = false;                    // radix-16 butterflies on the tensor cores
 };
 
-// The tunable choices of a plan: largest global-pass radix (multi-pass split)
-// and whether kernels run as persistent tile loops with L2 prefetch.
+// Both passes of a two-pass transform in one persistent launch whose queue
+// alternates first-pass tiles of transform b with second-pass tiles of
+// transform b - LAG, so that the intermediate is read back from L2
+// (fft_fused2.cu).
+struct Fused2Desc {
+    const void *fn = nullptr;
+    int threads = 0;
+    size_t smem = 0;
+    int logr1 = 0, logr2 = 0;
+    int ctas_per_sm = 0;
+};
+// Upper bound on the intermediates in flight between the two passes (bytes).
+constexpr uint64_t kFused2WindowBytes = 48ull << 20;
+
+// The tunable choices of a plan: largest global-pass radix (multi-pass split),
+// whether kernels run as persistent tile loops with L2 prefetch, and whether a
+// two-pass transform runs as one launch with an L2-resident intermediate.
 struct PlanVariant {
     int max_logr = 10;
     bool persistent = false;
+    bool fused = false;
     bool operator<(const PlanVariant &o) const {
-        return max_logr != o.max_logr ? max_logr < o.max_logr : persistent < o.persistent;
+        if (max_logr != o.max_logr) return max_logr < o.max_logr;
+        if (persistent != o.persistent) return persistent < o.persistent;
+        return fused < o.fused;
     }
-    bool operator==(const PlanVariant &o) const { return max_logr == o.max_logr && persistent == o.persistent; }
+    bool operator==(const PlanVariant &o) const {
+        return max_logr == o.max_logr && persistent == o.persistent && fused == o.fused;
+    }
 };
 
 struct Plan {
@@ -57,6 +77,8 @@ struct Plan {
     bool needs_workspace = false;
     RowsKernelInfo rows;
     std::vector<PassDesc> passes;
+    bool has_fused = false;  // variant.fused and a kernel exists for the two radices
+    Fused2Desc fused;
     // twiddle table (device): rows sub-pass tables, or for multi-pass the
     // per-pass sub-pass tables followed by the two-level W_N table.
     float2 *tw = nullptr;
@@ -83,6 +105,15 @@ cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uin
 cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
 constexpr size_t kTcGtabBytes = 4 * 2048;
 
+// fft_fused2.cu
+bool fused2_kernel_info(int logr1, int logr2, Fused2Desc &d);
+cudaError_t fused2_prepare(Fused2Desc &d);
+uint32_t fused2_lag(const Fused2Desc &d, int logn, uint64_t batch, int sms);
+cudaError_t fused2_launch(const Fused2Desc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
+                          const float2 *tw1, const float2 *tw2, const float2 *tw_lo, const float2 *tw_hi,
+                          int tw_split, float in_im, float out_re, float out_im, LoadOps ops, uint32_t *ctr,
+                          uint32_t *err, int sms, cudaStream_t stream);
+
 // log2 radices (each <= max_logr) of the global passes for a multi-pass
 // transform of 2^logn.
 std::vector<int> split_passes(int logn, int max_logr = 10);
@@ -99,10 +130,13 @@ uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t of
 std::vector<PlanVariant> plan_candidates(int logn, int precision);
 
 int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStream_t stream, std::string &why);
-// `err` is a device flag the tensor-core kernels raise when a bounded wait gives up.
-// `ops`: noise / window applied to every loaded input sample.
+// `err` is a device flag the tensor-core and fused kernels raise when a bounded
+// wait gives up.  `ops`: noise / window applied to every loaded input sample.
+// `ctr`: counter block of the fused two-pass form (grown and zeroed here; the
+// kernel leaves it zeroed); without it, or in place, the form falls back to
+// two launches.
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,
                  DeviceBuffer &ws, uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why,
-                 LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
+                 LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u}, DeviceBuffer *ctr = nullptr);
 
 }  // namespace gbfft

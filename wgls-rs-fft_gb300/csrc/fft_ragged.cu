@@ -8,17 +8,24 @@
 //   kind 0  G = 8192/N whole transforms of one size N <= 2^13 (single pass)
 //   kind 1  first global pass of a transform of N = 2^14 .. 2^18, 16*NG columns
 //   kind 2  second global pass of such a transform, 16*NG columns
-// Items are queued kind 1, then kind 0, then kind 2, and every CTA takes the
-// next item with one atomicAdd.  A kind-2 item depends on all kind-1 items of
-// its transform, which all sit earlier in the queue and are therefore already
-// owned by running CTAs that never wait: the wait always ends.  Each wait is
-// still bounded (spin_limit polls with __nanosleep): on expiry the kernel sets
-// an error flag, every CTA stops taking items, and the host reports
+// The queue mixes first passes and single-pass groups in proportion, and
+// places the second pass of each transform a fixed number of items after its
+// first pass (twice the CTAs in flight): late enough that it rarely waits,
+// early enough that the first pass's output, stored with normal L2 priority,
+// is still in L2 when it is read back.  Every CTA claims items in queue order
+// with one atomicAdd (the next claim is made while the current item runs).
+// A kind-2 item depends only on the kind-1 items of its transform, which sit
+// earlier in the queue; the oldest unfinished item is therefore always some
+// CTA's current item and can proceed, so every wait ends.  Each wait is still
+// bounded (spin_limit polls with __nanosleep): on expiry the kernel sets an
+// error flag, every CTA stops taking items, and the host reports
 // GBFFT_ERR_TIMEOUT.
 //
-// First-pass output goes to a workspace; producers publish with
-// __threadfence + atomicAdd, the consumer polls with ld.acquire.gpu and reads
-// the workspace with L1-bypassing loads.
+// Out of place, the first pass writes into the output buffer and the second
+// pass rewrites the same samples in place; in place, the first pass writes to
+// a workspace.  Producers publish with a CTA barrier, then one thread's
+// __threadfence + atomicAdd; the consumer polls with ld.acquire.gpu and reads
+// the intermediate with L1-bypassing loads.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -55,6 +62,7 @@ struct RagParams {
     const float2 *in;
     float2 *out;
     float2 *ws;
+    int p1_to_out;  // out of place: first-pass output goes to `out` (ws unused)
     const RagItem *items;
     uint32_t nitems;
     uint32_t spin_limit;
@@ -118,9 +126,10 @@ __device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, 
     }
     const bool inv = x.dir == GBFFT_INVERSE;
     const float sc = inv ? ldexpf(1.0f, -L) : 1.0f;
+    float2 *mid = P.p1_to_out ? P.out + x.offset : P.ws + x.ws_offset;
     PassArgs a;
-    a.src = FIRST ? P.in + x.offset : P.ws + x.ws_offset;
-    a.dst = FIRST ? P.ws + x.ws_offset : P.out + x.offset;
+    a.src = FIRST ? P.in + x.offset : mid;
+    a.dst = FIRST ? mid : P.out + x.offset;
     a.logn = L;
     a.logp = FIRST ? 0 : rag_logr1(L);
     a.col0 = it.b * (uint32_t)(kCols * NG);
@@ -132,14 +141,10 @@ __device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, 
     a.out_re = FIRST ? 1.0f : sc;
     a.out_im = FIRST ? 1.0f : (inv ? -sc : 1.0f);
     a.coherent_load = !FIRST;
+    a.keep_l2 = FIRST;
     a.row = 0;
     a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
     pass_tile<LOGR, NG, FIRST>(a, smem);
-    if (FIRST) {
-        __threadfence();  // this thread's workspace stores are visible GPU-wide
-        __syncthreads();
-        if (threadIdx.x == 0) atomicAdd(P.done1 + it.a, 1u);
-    }
     return true;
 }
 
@@ -154,17 +159,22 @@ __device__ __forceinline__ bool rag_pass_dispatch(const RagParams &P, const RagI
     }
 }
 
+__device__ __forceinline__ uint32_t rag_claim(const RagParams &P) {
+    return *(volatile uint32_t *)P.error != 0u ? 0xffffffffu : atomicAdd(P.item_counter, 1u);
+}
+
 __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P) {
     extern __shared__ float2 smem_rag[];
-    __shared__ uint32_t s_item;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const bool stop = *(volatile uint32_t *)P.error != 0u;
-            s_item = stop ? 0xffffffffu : atomicAdd(P.item_counter, 1u);
-        }
-        __syncthreads();
-        const uint32_t idx = s_item;
+    // Claimed queue positions, double-buffered: slot `par` holds the current
+    // item, slot par ^ 1 receives the next claim while the item runs.
+    __shared__ uint32_t s_item[2];
+    if (threadIdx.x == 0) s_item[0] = rag_claim(P);
+    __syncthreads();
+    for (uint32_t par = 0;; par ^= 1u) {
+        const uint32_t idx = s_item[par];
         if (idx >= P.nitems) break;
+        // (slot par ^ 1 was last read before the previous item's final barrier)
+        if (threadIdx.x == 0) s_item[par ^ 1u] = rag_claim(P);
         const RagItem it = P.items[idx];
         bool ok = true;
         if (it.kind == 0) {
@@ -183,7 +193,12 @@ __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P)
             ok = rag_pass_dispatch<false>(P, it, smem_rag);
         }
         if (!ok) break;
-        __syncthreads();  // shared memory and s_item are reused by the next item
+        __syncthreads();  // the item's stores are issued; shared memory is free
+        if (it.kind == 1 && threadIdx.x == 0) {
+            // publish: the barrier ordered the CTA's stores before this fence
+            __threadfence();
+            atomicAdd(P.done1 + it.a, 1u);
+        }
     }
 }
 
@@ -246,23 +261,21 @@ struct RaggedPlanImpl {
     cudaStream_t capture_stream = nullptr;
     uint64_t launches = 0;
     int sms = 0;
+    bool prepared = false;  // kernel attributes set
 };
 
 static void build_items(RaggedPlanImpl &p) {
     p.items.clear();
     p.order.clear();
+    // kind 0: groups of whole transforms of one size, largest sizes first
     std::vector<std::vector<uint32_t>> by_size(kRagRowsMaxLogN + 1);
-    // kind 1 first
+    std::vector<uint32_t> two;  // two-pass transforms, in descriptor order
     for (uint32_t i = 0; i < p.count; ++i) {
         const RagXform &x = p.xf[i];
-        if (x.logn > kRagRowsMaxLogN) {
-            if (p.drop_producers) continue;  // test hook: nothing will publish the first pass
-            for (uint32_t t = 0; t < x.tiles1; ++t) p.items.push_back(RagItem{1, i, t, (uint32_t)x.logn});
-        } else {
-            by_size[x.logn].push_back(i);
-        }
+        if (x.logn > kRagRowsMaxLogN) two.push_back(i);
+        else by_size[x.logn].push_back(i);
     }
-    // kind 0, largest sizes first
+    std::vector<RagItem> rows;
     for (int L = kRagRowsMaxLogN; L >= 0; --L) {
         const uint32_t g = (uint32_t)(kRagThreads / (1 << (L < 4 ? 0 : L - 4)));
         const std::vector<uint32_t> &ids = by_size[L];
@@ -270,18 +283,36 @@ static void build_items(RaggedPlanImpl &p) {
             const uint32_t first = (uint32_t)p.order.size();
             const uint32_t n = (uint32_t)std::min<size_t>(g, ids.size() - s);
             for (uint32_t k = 0; k < n; ++k) p.order.push_back(ids[s + k]);
-            p.items.push_back(RagItem{0, first, n, (uint32_t)L});
+            rows.push_back(RagItem{0, first, n, (uint32_t)L});
         }
     }
-    // kind 2 last
-    for (uint32_t i = 0; i < p.count; ++i) {
+    uint64_t total_p1 = 0;
+    for (uint32_t i : two) total_p1 += p.xf[i].tiles1;
+    // the second pass of a transform follows its first pass by `lag` items
+    const uint64_t lag = 4ull * (uint64_t)std::max(1, p.sms);
+    std::vector<std::pair<uint32_t, uint64_t>> pending;  // (transform, release position), FIFO
+    size_t head = 0, ri = 0;
+    uint64_t p1_seen = 0;
+    auto emit_p2 = [&](uint32_t i) {
         const RagXform &x = p.xf[i];
-        if (x.logn > kRagRowsMaxLogN) {
-            const int lr2 = rag_logr2(x.logn);
-            const uint32_t tiles2 = (1u << (x.logn - lr2)) / (uint32_t)(kCols * rag_groups(lr2));
-            for (uint32_t t = 0; t < tiles2; ++t) p.items.push_back(RagItem{2, i, t, (uint32_t)x.logn});
-        }
+        const int lr2 = rag_logr2(x.logn);
+        const uint32_t tiles2 = (1u << (x.logn - lr2)) / (uint32_t)(kCols * rag_groups(lr2));
+        for (uint32_t t = 0; t < tiles2; ++t) p.items.push_back(RagItem{2, i, t, (uint32_t)x.logn});
+    };
+    for (uint32_t i : two) {
+        while (head < pending.size() && pending[head].second <= p.items.size()) emit_p2(pending[head++].first);
+        const RagXform &x = p.xf[i];
+        // test hook: nothing will publish the first pass
+        if (!p.drop_producers)
+            for (uint32_t t = 0; t < x.tiles1; ++t) p.items.push_back(RagItem{1, i, t, (uint32_t)x.logn});
+        p1_seen += x.tiles1;
+        pending.emplace_back(i, (uint64_t)p.items.size() + lag);
+        // single-pass groups in proportion to the first passes issued so far
+        const size_t want = (size_t)((double)rows.size() * (double)p1_seen / (double)total_p1);
+        while (ri < want && ri < rows.size()) p.items.push_back(rows[ri++]);
     }
+    while (ri < rows.size()) p.items.push_back(rows[ri++]);
+    while (head < pending.size()) emit_p2(pending[head++].first);
     if (p.order.empty()) p.order.push_back(0);
     p.nitems = (uint32_t)p.items.size();
     p.dirty = true;
@@ -292,6 +323,7 @@ int ragged_plan_build(RaggedPlanImpl *&out, int device, const gbfft_ragged_desc 
     out = nullptr;
     RaggedPlanImpl *p = new RaggedPlanImpl();
     p->device = device;
+    cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, device);
     p->count = count;
     p->xf.resize(count);
     uint64_t ws = 0;
@@ -357,9 +389,9 @@ int ragged_plan_build(RaggedPlanImpl *&out, int device, const gbfft_ragged_desc 
     return GBFFT_OK;
 }
 
-int ragged_plan_upload(RaggedPlanImpl &p, cudaStream_t stream, std::string &why) {
-    if (p.sms == 0) {
-        cudaDeviceGetAttribute(&p.sms, cudaDevAttrMultiProcessorCount, p.device);
+int ragged_plan_upload(RaggedPlanImpl &p, bool in_place, cudaStream_t stream, std::string &why) {
+    if (!p.prepared) {
+        p.prepared = true;
         cudaError_t e = cudaFuncSetAttribute((const void *)fft_ragged_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rag_smem_bytes());
         if (e != cudaSuccess) {
@@ -387,7 +419,7 @@ int ragged_plan_upload(RaggedPlanImpl &p, cudaStream_t stream, std::string &why)
             }
         }
     }
-    if (p.ws_samples > 0) {
+    if (in_place && p.ws_samples > 0) {  // out of place, the first pass writes into the output
         int st = p.ws.ensure(p.ws_samples * sizeof(float2), why);
         if (st != GBFFT_OK) return st;
     }
@@ -422,6 +454,7 @@ static RagParams rag_params(const RaggedPlanImpl &p, const void *in, void *out) 
     P.in = (const float2 *)in;
     P.out = (float2 *)out;
     P.ws = (float2 *)p.ws.ptr;
+    P.p1_to_out = in != (const void *)out;
     P.items = (const RagItem *)(m + p.off_items);
     P.nitems = p.nitems;
     P.spin_limit = p.spin_limit;
@@ -459,7 +492,7 @@ static cudaError_t rag_enqueue(RaggedPlanImpl &p, const void *in, void *out, cud
 
 int ragged_plan_execute(RaggedPlanImpl &p, const void *in, void *out, cudaStream_t stream, bool use_graph,
                         std::string &why) {
-    int st = ragged_plan_upload(p, stream, why);
+    int st = ragged_plan_upload(p, in == (const void *)out, stream, why);
     if (st != GBFFT_OK) return st;
     cudaError_t e;
     if (!use_graph) {

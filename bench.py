@@ -317,7 +317,9 @@ def run_ragged(args, ctx, dev, rank, world):
                        "directions": "50/50", "total_samples": total, "form": "fp32 ragged persistent (graph)",
                        "l2": "inputs (4 GB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                         "frac": achieved / peak,
+                         "traffic": profile_traffic("ragged_c5") if args.ragged_count == 10000 else None,
+                         "peak_source": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "executed_bytes_per_launch": exec_bytes,
                          "launch_us": ms * 1e3 / max(1, launches)},
             "uniform_batches": {"value": uvalue, "unit": UNIT, "launches_per_step": len(calls),

@@ -66,7 +66,7 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
     std::vector<PlanVariant> c;
     if (logn <= kRowsMaxLogN) {
         // one CTA per SM leaves no other CTA to overlap with: prefetch helps
-        const bool big = logn >= 13;
+        const bool big = logn >= 14;
         c.push_back(PlanVariant{10, big});
         c.push_back(PlanVariant{10, !big});
         return c;

@@ -198,6 +198,30 @@ def cpu_reference_rate(logn, batch, rows, seconds_budget, threads):
     return 2.0 * rows * n * reps / el / 1e9, rows, reps
 
 
+def cpu_library_rate(logn, batch, rows, seconds_budget):
+    """scipy.fft (pocketfft) complex64 on all host threads over `rows` rows,
+    forward + inverse: an optimised CPU FFT reported beside the reference's
+    own path (rustfft, the reference tests' comparator, cannot be built
+    here).  Returns (GSamples/s, rows, reps) or None without scipy."""
+    try:
+        import scipy.fft as sfft
+    except ImportError:
+        return None
+    from gbfft import signals
+    n = 1 << logn
+    rows = max(1, min(rows, batch))
+    x = signals.normal_c64(rows, n, seed=2)
+    sfft.ifft(sfft.fft(x, axis=1, workers=-1), axis=1, workers=-1)  # warm
+    reps, t0 = 0, time.perf_counter()
+    while True:
+        sfft.ifft(sfft.fft(x, axis=1, workers=-1), axis=1, workers=-1)
+        reps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds_budget:
+            break
+    return 2.0 * rows * n * reps / el / 1e9, rows, reps
+
+
 def run_reference_arm(args, workload):
     rank, world, _ = rank_info()
     if rank != 0:
@@ -247,7 +271,11 @@ def run_ragged(args, ctx, dev, rank, world):
     descs, total = signals.ragged_set(args.ragged_count, seed=5)
     x = signals.uniform_c64_torch(1, total, seed=5, device=dev)[0]
     y = torch.empty_like(x)
+    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3}[args.precision]
+    ctx.set_precision(prec)  # the plan takes the context's precision
     plan = ctx.ragged_plan(descs)
+    # the uniform comparison: the split form where the uniform entry has it (N >= 2^15)
+    ctx_small = gbfft.Context(dev.index or 0)
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
     sampler = ClockSampler(dev.index or 0)
@@ -289,7 +317,7 @@ def run_ragged(args, ctx, dev, rank, world):
 
     def uniform_step():
         for p0, n, b, d in calls:
-            ctx.c2c_device(xu[p0:], yu[p0:], n, b, d, stream=sp)
+            (ctx if n >= (1 << 15) else ctx_small).c2c_device(xu[p0:], yu[p0:], n, b, d, stream=sp)
     for _ in range(max(3, args.warmup)):
         uniform_step()
     torch.cuda.synchronize(dev)
@@ -301,6 +329,20 @@ def run_ragged(args, ctx, dev, rank, world):
     torch.cuda.synchronize(dev)
     ums = ev0.elapsed_time(ev1)
     uvalue = total * usteps / (ums * 1e-3) / 1e9
+
+    # one transform of every size against a float64 FFT (checker only)
+    plan.execute(x, y, total, use_graph=True, stream=sp)
+    plan.wait(stream=sp)
+    worst, seen = 0.0, set()
+    for off, L, d in descs.tolist():
+        if L in seen:
+            continue
+        seen.add(L)
+        xs = x[off:off + (1 << L)].to(torch.complex128)
+        ref = torch.fft.ifft(xs) if d == 1 else torch.fft.fft(xs)
+        err = (torch.linalg.vector_norm(y[off:off + (1 << L)].to(torch.complex128) - ref)
+               / torch.linalg.vector_norm(ref)).item()
+        worst = max(worst, err)
 
     sv_pass = lambda L: 1 if L <= 14 else 2  # graded accounting: 1 pass up to 2^14
     alg_bytes = sum(16 * (1 << L) * sv_pass(L) for L in descs["log2n"].tolist())
@@ -314,7 +356,8 @@ def run_ragged(args, ctx, dev, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PCG hash, re/im iid U[-1,1))",
             "config": {"workload": "ragged_c5", "transforms": len(descs), "log2n": "uniform 8..18",
-                       "directions": "50/50", "total_samples": total, "form": "fp32 ragged persistent (graph)",
+                       "directions": "50/50", "total_samples": total, "precision": args.precision,
+                       "form": f"{args.precision} ragged persistent (graph)",
                        "l2": "inputs (4 GB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
@@ -326,9 +369,12 @@ def run_ragged(args, ctx, dev, rank, world):
                                 "ragged_over_uniform": value / uvalue},
             "cpu_baseline": None, "e2e": None, "gpu_launches": launches,
             "clocks": sampler.summary(),
+            "accuracy": {"precision": args.precision, "max_rel_l2_vs_fp64": worst, "sizes_checked": len(seen),
+                         "reference": "float64 torch.fft of one transform per size (checker only)"},
         }
         print(json.dumps(line), flush=True)
     plan.close()
+    ctx_small.close()
     return 0
 
 
@@ -477,7 +523,7 @@ def main():
                "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
                "steps": args.e2e_steps, "api": "gbfft_c2c_host (pinned host buffers)"}
 
-    cpu = None
+    cpu = cpu_lib = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rows = 256 if n <= 4096 else max(1, (1 << 20) // n)
@@ -485,6 +531,11 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{rows} of {batch} rows of N={n}, forward+inverse, repeated {reps}x "
                          f"(~{args.cpu_seconds:.0f} s); reference Stockham R4/R2 f32 path restated in C"}
+        lib = cpu_library_rate(logn, batch, rows, min(args.cpu_seconds, 5.0))
+        if lib is not None:
+            cpu_lib = {"value": lib[0], "unit": UNIT, "cores": threads,
+                       "library": "scipy.fft (pocketfft) complex64, workers=-1",
+                       "sample": f"{lib[1]} of {batch} rows of N={n}, forward+inverse, repeated {lib[2]}x"}
 
     if rank == 0:
         line = {
@@ -507,7 +558,9 @@ def main():
                                        f"{launches_per_transform:g} launch(es) per transform",
                          "dram_floor_frac": floor_achieved / peak},
             "cpu_baseline": cpu,
+            "cpu_fft_library": cpu_lib,
             "cufft_baseline": cufft,
+            "gflops": value * 5 * logn,  # 5 N log2 N flops per transform (the reference's model)
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": sampler.summary(),

@@ -171,3 +171,66 @@ def test_ragged_full_workload_roundtrip(gpu_ctx, oracle, torch):
     assert len(seen) == 11
     plan.close()
     back.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5)])
+def test_ragged_split_tensor_core_form(lib_built, oracle, torch, prec, tol):
+    """The ragged launch in the split tensor-core forms (the context's
+    precision when the plan is made): two-pass transforms (N = 2^14..2^18) run
+    their radix-16 butterflies on tcgen05, single-pass ones stay FP32.  Gates
+    as for the uniform split form: FP16 hi+lo at rel-L2 <= 2e-6 against FP64,
+    BF16x3 at 2e-5; graph replay repeats the result exactly; in place works."""
+    import gbfft
+    from gbfft import signals
+    rng = np.random.default_rng(8)
+    sizes = list(range(8, 19)) + [int(v) for v in rng.integers(12, 19, size=20)]
+    dirs = [int(v) for v in rng.choice([-1, 1], size=len(sizes))]
+    descs, total = _mixed_descs(sizes, dirs)
+    x = signals.uniform_c64(1, total, seed=45)[0]
+    with gbfft.Context(0) as ctx:
+        ctx.set_precision(prec)
+        d_in = torch.from_numpy(x).cuda()
+        d_out = torch.full_like(d_in, float("nan"))
+        plan = ctx.ragged_plan(descs)
+        plan.execute(d_in, d_out, total, use_graph=True)
+        plan.wait()
+        y = d_out.cpu().numpy()
+        for off, L, d in descs.tolist():
+            n = 1 << L
+            ref = oracle.fft64(x[off:off + n][None, :], inverse=(d == 1))[0]
+            assert oracle.rel_l2(y[off:off + n], ref) <= tol, (L, d)
+        plan.execute(d_in, d_out, total, use_graph=True)
+        plan.wait()
+        assert np.array_equal(d_out.cpu().numpy(), y, equal_nan=True)  # gaps stay NaN
+        d_io = d_in.clone()
+        plan.execute(d_io, d_io, total, use_graph=False)
+        plan.wait()
+        assert np.array_equal(d_io.cpu().numpy()[~np.isnan(y)], y[~np.isnan(y)])
+        plan.close()
+
+
+def test_ragged_split_form_wait_times_out(lib_built, torch):
+    """The dropped-producer failure path in the tensor-core ragged kernel: the
+    bounded dependency wait gives up, GBFFT_ERR_TIMEOUT is reported, TMEM is
+    released and the context keeps working."""
+    import gbfft
+    from gbfft import signals
+    descs, total = _mixed_descs([15, 17, 9], [-1, 1, -1])
+    x = signals.uniform_c64(1, total, seed=46)[0]
+    with gbfft.Context(0) as ctx:
+        ctx.set_precision(gbfft.PREC_TC_FP16)
+        d = torch.from_numpy(x).cuda()
+        o = torch.zeros_like(d)
+        plan = ctx.ragged_plan(descs)
+        plan.set(gbfft.RAGGED_OPT_SPIN_LIMIT, 2000)
+        plan.set(gbfft.RAGGED_OPT_TEST_DROP_PRODUCERS, 1)
+        plan.execute(d, o, total, use_graph=False)
+        with pytest.raises(gbfft.GbfftError) as e:
+            plan.wait()
+        assert e.value.status == gbfft.ERR_TIMEOUT
+        plan.set(gbfft.RAGGED_OPT_TEST_DROP_PRODUCERS, 0)
+        plan.execute(d, o, total, use_graph=False)
+        plan.wait()
+        plan.close()
+        ctx.set_precision(gbfft.PREC_FP32)
+        assert np.isfinite(ctx.c2c_host(x[:256][None, :], gbfft.FORWARD)).all()

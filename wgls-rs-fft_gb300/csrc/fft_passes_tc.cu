@@ -20,18 +20,6 @@
 
 namespace gbfft {
 
-template <bool BF16>
-struct DftTc {
-    TcState *s;
-    template <int R>
-    __device__ __forceinline__ void run(float2 (&x)[R]) {
-        if constexpr (R == 16) tc_dft16<BF16>(x, *s);
-        else Dft<R>::run(x);
-    }
-};
-
-constexpr uint32_t kTcSpinLimit = 1u << 20;  // polls of an MMA completion that takes microseconds
-
 // Column groups per CTA: enough threads (>= 128) to fill one M = 128 MMA.
 template <int LOGR>
 constexpr int tc_groups() {

@@ -34,6 +34,7 @@
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"
 #include "gbfft_ragged.h"
+#include "fft_tc.cuh"
 #include "fft_tiles.cuh"
 
 namespace gbfft {
@@ -100,9 +101,10 @@ __device__ __forceinline__ void rag_rows(const RagParams &P, const RagItem &it, 
     rows_tile<L, G>(ref, P.sub[L], smem, LoadOps{nullptr, 0u, 0.f, 0u});
 }
 
-// Returns false when the wait for the first pass gave up.
-template <int LOGR, bool FIRST>
-__device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, float2 *smem) {
+// Returns false when the wait for the first pass gave up.  Eng: the
+// butterfly engine (FP32 registers, or the tensor-core split form).
+template <int LOGR, bool FIRST, class Eng>
+__device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, float2 *smem, Eng &eng) {
     constexpr int NG = rag_groups(LOGR);
     __shared__ int s_abort;
     const RagXform x = P.xf[it.a];
@@ -144,17 +146,17 @@ __device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, 
     a.keep_l2 = FIRST;
     a.row = 0;
     a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
-    pass_tile<LOGR, NG, FIRST>(a, smem);
+    pass_tile<LOGR, NG, FIRST, Eng>(a, smem, eng);
     return true;
 }
 
-template <bool FIRST>
-__device__ __forceinline__ bool rag_pass_dispatch(const RagParams &P, const RagItem &it, float2 *smem) {
+template <bool FIRST, class Eng>
+__device__ __forceinline__ bool rag_pass_dispatch(const RagParams &P, const RagItem &it, float2 *smem, Eng &eng) {
     const int logr = FIRST ? rag_logr1(it.logn) : rag_logr2(it.logn);
     switch (logr) {
-        case 7: return rag_pass<7, FIRST>(P, it, smem);
-        case 8: return rag_pass<8, FIRST>(P, it, smem);
-        case 9: return rag_pass<9, FIRST>(P, it, smem);
+        case 7: return rag_pass<7, FIRST>(P, it, smem, eng);
+        case 8: return rag_pass<8, FIRST>(P, it, smem, eng);
+        case 9: return rag_pass<9, FIRST>(P, it, smem, eng);
         default: return true;
     }
 }
@@ -163,8 +165,10 @@ __device__ __forceinline__ uint32_t rag_claim(const RagParams &P) {
     return *(volatile uint32_t *)P.error != 0u ? 0xffffffffu : atomicAdd(P.item_counter, 1u);
 }
 
-__global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P) {
-    extern __shared__ float2 smem_rag[];
+// The queue loop shared by the FP32 and tensor-core kernels.  Single-pass
+// groups always run on the FP32 pipes; two-pass items use `eng`.
+template <class Eng>
+__device__ __forceinline__ void rag_loop(const RagParams &P, float2 *smem_rag, Eng &eng) {
     // Claimed queue positions, double-buffered: slot `par` holds the current
     // item, slot par ^ 1 receives the next claim while the item runs.
     __shared__ uint32_t s_item[2];
@@ -188,9 +192,9 @@ __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P)
                 default: break;
             }
         } else if (it.kind == 1) {
-            ok = rag_pass_dispatch<true>(P, it, smem_rag);
+            ok = rag_pass_dispatch<true>(P, it, smem_rag, eng);
         } else {
-            ok = rag_pass_dispatch<false>(P, it, smem_rag);
+            ok = rag_pass_dispatch<false>(P, it, smem_rag, eng);
         }
         if (!ok) break;
         __syncthreads();  // the item's stores are issued; shared memory is free
@@ -200,6 +204,73 @@ __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P)
             atomicAdd(P.done1 + it.a, 1u);
         }
     }
+}
+
+// (gtab and off_g are the tensor-core kernel's; both kernels take the same arguments)
+__global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P, const uint4 *, uint32_t) {
+    extern __shared__ float2 smem_rag[];
+    DftRegs eng;
+    rag_loop(P, smem_rag, eng);
+}
+
+// Tensor-core split form.  Shared memory: the item region (FP32 exchange
+// tile + column twiddles, or a rows tile; the hi/lo A operands alias the
+// exchange tile while a tensor-core DFT runs), then the two G operand parts,
+// then the mbarrier.  TMEM (32 columns per 128 threads) is allocated once for
+// the CTA's whole run.
+struct RagTcLayout {
+    static constexpr int NMMA = kRagThreads / 128;
+    static constexpr uint32_t TMEM_COLS = 128;
+    static constexpr size_t A_BYTES = (size_t)kRagThreads * kTcRowBytes;
+    static_assert(NMMA * 32 <= (int)TMEM_COLS, "TMEM columns");
+    static_assert(2 * A_BYTES <= (size_t)kRagThreads * 16 * sizeof(float2), "A operands fit in the exchange tile");
+};
+
+template <bool BF16>
+__global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_tc_kernel(RagParams P, const uint4 *__restrict__ gtab,
+                                                                       uint32_t off_g) {
+    using Lay = RagTcLayout;
+    extern __shared__ __align__(1024) uint8_t smem_rtc[];
+    uint64_t *bar = (uint64_t *)(smem_rtc + off_g + 2 * kTcGBytes);
+    uint32_t *s_taddr = (uint32_t *)(smem_rtc + off_g + 2 * kTcGBytes + 8);
+    int *s_abort = (int *)(smem_rtc + off_g + 2 * kTcGBytes + 12);
+    const int tid = threadIdx.x;
+    const uint4 *gsrc = gtab + (BF16 ? 2 : 0) * (kTcGBytes / 16);
+    uint4 *gdst = (uint4 *)(smem_rtc + off_g);
+    for (int i = tid; i < 2 * kTcGBytes / 16; i += kRagThreads) gdst[i] = gsrc[i];
+    if (tid < 32) tmem_alloc(s_taddr, Lay::TMEM_COLS);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        *s_abort = 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    TcState st;
+    st.a_hi = smem_rtc;
+    st.a_lo = smem_rtc + Lay::A_BYTES;
+    st.g_hi = smem_rtc + off_g;
+    st.g_lo = smem_rtc + off_g + kTcGBytes;
+    st.bar = bar;
+    st.abort = s_abort;
+    st.err = P.error;  // a completion wait that gives up stops the whole launch
+    st.taddr = *s_taddr;
+    st.parity = 0;
+    st.nmma = Lay::NMMA;
+    st.spin_limit = kTcSpinLimit;
+    DftTc<BF16> eng{&st};
+    rag_loop(P, (float2 *)smem_rtc, eng);
+
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0 && *s_abort) {
+        // a wait gave up: let the MMAs that were issued finish before freeing TMEM
+        for (uint32_t polls = 0; polls < kTcSpinLimit && !mbar_try_wait(bar, st.parity ^ 1u); ++polls) {
+        }
+    }
+    __syncthreads();
+    tc_fence_after();
+    if (tid < 32) tmem_dealloc(st.taddr, Lay::TMEM_COLS);
 }
 
 // ---------------------------------------------------------------------------
@@ -262,7 +333,22 @@ struct RaggedPlanImpl {
     uint64_t launches = 0;
     int sms = 0;
     bool prepared = false;  // kernel attributes set
+    int precision = GBFFT_PREC_FP32;
+    void *gtab = nullptr;   // split form: the G operand parts (fft_passes_tc.cu)
 };
+
+static size_t rag_tc_off_g() { return (rag_smem_bytes() + 1023) & ~(size_t)1023; }
+static size_t rag_tc_smem_bytes() { return rag_tc_off_g() + 2 * kTcGBytes + 64; }
+static const void *rag_kernel(const RaggedPlanImpl &p) {
+    switch (p.precision) {
+        case GBFFT_PREC_TC_FP16: return (const void *)fft_ragged_tc_kernel<false>;
+        case GBFFT_PREC_TC_BF16X3: return (const void *)fft_ragged_tc_kernel<true>;
+        default: return (const void *)fft_ragged_kernel;
+    }
+}
+static size_t rag_kernel_smem(const RaggedPlanImpl &p) {
+    return p.precision == GBFFT_PREC_FP32 ? rag_smem_bytes() : rag_tc_smem_bytes();
+}
 
 static void build_items(RaggedPlanImpl &p) {
     p.items.clear();
@@ -319,10 +405,11 @@ static void build_items(RaggedPlanImpl &p) {
 }
 
 int ragged_plan_build(RaggedPlanImpl *&out, int device, const gbfft_ragged_desc *descs, uint32_t count,
-                      std::string &why) {
+                      int precision, std::string &why) {
     out = nullptr;
     RaggedPlanImpl *p = new RaggedPlanImpl();
     p->device = device;
+    p->precision = precision;
     cudaDeviceGetAttribute(&p->sms, cudaDevAttrMultiProcessorCount, device);
     p->count = count;
     p->xf.resize(count);
@@ -391,13 +478,17 @@ int ragged_plan_build(RaggedPlanImpl *&out, int device, const gbfft_ragged_desc 
 
 int ragged_plan_upload(RaggedPlanImpl &p, bool in_place, cudaStream_t stream, std::string &why) {
     if (!p.prepared) {
-        p.prepared = true;
-        cudaError_t e = cudaFuncSetAttribute((const void *)fft_ragged_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rag_smem_bytes());
+        cudaError_t e = cudaFuncSetAttribute(rag_kernel(p), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)rag_kernel_smem(p));
+        if (e == cudaSuccess && p.precision != GBFFT_PREC_FP32) {
+            e = cudaMalloc(&p.gtab, kTcGtabBytes);
+            if (e == cudaSuccess) e = tc_gtab_fill(p.gtab, stream);
+        }
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;
         }
+        p.prepared = true;
     }
     if (!p.h_error) {
         if (cudaHostAlloc(&p.h_error, sizeof(uint32_t), cudaHostAllocDefault) != cudaSuccess) {
@@ -482,8 +573,10 @@ static cudaError_t rag_enqueue(RaggedPlanImpl &p, const void *in, void *out, cud
     RagParams P = rag_params(p, in, out);
     if (p.nitems > 0) {
         const unsigned grid = (unsigned)std::max(1, std::min<int>(2 * p.sms, (int)p.nitems));
-        void *args[] = {(void *)&P};
-        e = cudaLaunchKernel((const void *)fft_ragged_kernel, dim3(grid), dim3(kRagThreads), args, rag_smem_bytes(), s);
+        const uint4 *gtab = (const uint4 *)p.gtab;
+        uint32_t off_g = (uint32_t)rag_tc_off_g();
+        void *args[] = {(void *)&P, (void *)&gtab, (void *)&off_g};
+        e = cudaLaunchKernel(rag_kernel(p), dim3(grid), dim3(kRagThreads), args, rag_kernel_smem(p), s);
         if (e != cudaSuccess) return e;
     }
     return cudaMemcpyAsync(p.h_error, m + p.off_counters + sizeof(uint32_t), sizeof(uint32_t),
@@ -584,6 +677,7 @@ void ragged_plan_free(RaggedPlanImpl *p) {
     if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->capture_stream) cudaStreamDestroy(p->capture_stream);
+    if (p->gtab) cudaFree(p->gtab);
     if (p->h_error) cudaFreeHost(p->h_error);
     delete p;
 }

@@ -26,6 +26,8 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include "fft_core.cuh"
+
 namespace gbfft {
 
 constexpr int kTcRowBytes = 64;        // 32 16-bit values
@@ -240,5 +242,19 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
 #pragma unroll
     for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]) * up, __uint_as_float(d[16 + q]) * up);
 }
+
+// Butterfly engine for pass_tile / rows_tile: radix-16 butterflies on the
+// tensor cores, the radix 2/4/8 remainder on the FP32 pipes.
+template <bool BF16>
+struct DftTc {
+    TcState *s;
+    template <int R>
+    __device__ __forceinline__ void run(float2 (&x)[R]) {
+        if constexpr (R == 16) tc_dft16<BF16>(x, *s);
+        else Dft<R>::run(x);
+    }
+};
+
+constexpr uint32_t kTcSpinLimit = 1u << 20;  // polls of an MMA completion that takes microseconds
 
 }  // namespace gbfft

@@ -546,7 +546,7 @@ int gbfft_ragged_plan_create(gbfft_ctx *ctx, const gbfft_ragged_desc *descs, uin
     GB_CUDA(ctx, cudaSetDevice(ctx->device));
     RaggedPlanImpl *impl = nullptr;
     std::string why;
-    int st = ragged_plan_build(impl, ctx->device, descs, count, why);
+    int st = ragged_plan_build(impl, ctx->device, descs, count, ctx->precision, why);
     if (st != GBFFT_OK) return fail(ctx, st, "%s", why.c_str());
     *out_plan = new gbfft_ragged_plan{ctx, impl};
     return GBFFT_OK;

@@ -8,8 +8,10 @@ namespace gbfft {
 
 struct RaggedPlanImpl;
 
+// precision: GBFFT_PREC_*; the split forms run the two-pass transforms
+// (N = 2^14 .. 2^18) on the tensor cores, the single-pass ones in FP32.
 int ragged_plan_build(RaggedPlanImpl *&out, int device, const gbfft_ragged_desc *descs, uint32_t count,
-                      std::string &why);
+                      int precision, std::string &why);
 int ragged_plan_execute(RaggedPlanImpl &p, const void *in, void *out, cudaStream_t stream, bool use_graph,
                         std::string &why);
 int ragged_plan_wait(RaggedPlanImpl &p, cudaStream_t stream, std::string &why);

@@ -51,7 +51,6 @@ struct Fused2Params {
     const float2 *in;
     float2 *out;
     uint32_t batch;
-    uint32_t tiles;   // tiles per pass per transform (both passes move 16 x THREADS samples a tile)
     uint32_t lag;     // min(LAG, batch)
     uint32_t nitems;  // 2 x tiles x batch
     int logn;
@@ -71,10 +70,11 @@ __device__ __forceinline__ uint32_t f2_ld_acquire(const uint32_t *p) {
     return v;
 }
 
-// Queue position -> (pass, transform, tile).
+// Queue position -> (pass, transform, tile); T tiles per pass per transform.
+template <uint32_t T>
 __device__ __forceinline__ void fused2_item(const Fused2Params &P, uint32_t idx, bool &first, uint32_t &b,
                                             uint32_t &tile) {
-    const uint32_t T = P.tiles, L = P.lag;
+    const uint32_t L = P.lag;
     const uint32_t pro = L * T;
     if (idx < pro) {
         first = true;
@@ -106,6 +106,8 @@ template <int LOGR1, int LOGR2, int THREADS>
 __global__ void __launch_bounds__(THREADS, Fused2Cfg<LOGR1, LOGR2, THREADS>::MINB)
 fft_fused2_kernel(Fused2Params P) {
     using C = Fused2Cfg<LOGR1, LOGR2, THREADS>;
+    constexpr int LOGN = LOGR1 + LOGR2;
+    constexpr uint32_t T = (1u << LOGN) / (16u * THREADS);
     extern __shared__ float2 smem_f2[];
     // Claimed queue positions, double-buffered: slot `par` holds the current
     // item, slot par ^ 1 receives the next claim while the tile runs.
@@ -124,10 +126,10 @@ fft_fused2_kernel(Fused2Params P) {
         if (threadIdx.x == 0) s_item[par ^ 1u] = fused2_claim(P);
         bool first;
         uint32_t b, tile;
-        fused2_item(P, idx, first, b, tile);
-        const uint64_t base = (uint64_t)b << P.logn;
+        fused2_item<T>(P, idx, first, b, tile);
+        const uint64_t base = (uint64_t)b << LOGN;
         PassArgs a;
-        a.logn = P.logn;
+        a.logn = LOGN;
         a.tw_lo = P.tw_lo;
         a.tw_hi = P.tw_hi;
         a.tw_split = P.tw_split;
@@ -144,12 +146,12 @@ fft_fused2_kernel(Fused2Params P) {
             a.coherent_load = false;
             a.keep_l2 = true;
             a.ops = P.ops;
-            pass_tile<LOGR1, C::NG1, true>(a, smem_f2);
+            pass_tile<LOGR1, C::NG1, true, DftRegs, LOGR1 + LOGR2, 0>(a, smem_f2);
         } else {
             if (threadIdx.x == 0) {
                 uint32_t polls = 0;
                 int abort = 0;
-                while (f2_ld_acquire(P.ctr + 2 + b) < P.tiles) {
+                while (f2_ld_acquire(P.ctr + 2 + b) < T) {
                     if (++polls > P.spin_limit) {
                         atomicExch(P.err, 1u);
                         abort = 1;
@@ -171,11 +173,11 @@ fft_fused2_kernel(Fused2Params P) {
             a.out_im = P.out_im;
             a.coherent_load = true;
             a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
-            pass_tile<LOGR2, C::NG2, false>(a, smem_f2);
+            pass_tile<LOGR2, C::NG2, false, DftRegs, LOGR1 + LOGR2, LOGR1>(a, smem_f2);
         }
         __syncthreads();  // the tile's stores are issued; shared memory is free
         if (threadIdx.x == 0) {
-            fused2_item(P, idx, first, b, tile);  // recomputed: nothing stays live across the tile
+            fused2_item<T>(P, idx, first, b, tile);  // recomputed: nothing stays live across the tile
             if (first) {
                 // publish: the barrier ordered the CTA's stores before this fence
                 __threadfence();
@@ -253,9 +255,9 @@ cudaError_t fused2_launch(const Fused2Desc &d, const float2 *in, float2 *out, ui
     P.in = in;
     P.out = out;
     P.batch = (uint32_t)batch;
-    P.tiles = (uint32_t)((1ull << logn) / (16ull * (uint64_t)d.threads));
+    const uint32_t tiles = (uint32_t)((1ull << logn) / (16ull * (uint64_t)d.threads));  // per pass per transform
     P.lag = fused2_lag(d, logn, batch, sms);
-    P.nitems = 2u * P.tiles * P.batch;
+    P.nitems = 2u * tiles * P.batch;
     P.logn = logn;
     P.tw1 = tw1;
     P.tw2 = tw2;

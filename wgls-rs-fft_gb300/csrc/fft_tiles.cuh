@@ -162,7 +162,10 @@ struct PassArgs {
 };
 
 // NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
-template <int LOGR, int NG, bool FIRST, class Eng = DftRegs>
+// LOGN_CT / LOGP_CT: log2 N and log2 p when the caller knows them at compile
+// time (0 / -1: taken from a.logn / a.logp).  Constant sizes turn every
+// strided address and twiddle index into immediates.
+template <int LOGR, int NG, bool FIRST, class Eng = DftRegs, int LOGN_CT = 0, int LOGP_CT = -1>
 __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng eng = Eng()) {
     using C = SubCfg<LOGR>;
     using K = PassTileCfg<LOGR, NG>;
@@ -174,7 +177,10 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
     const int t = lt >> kColsLog;
     float2 *buf = smem + grp * (kCols * R);
     float2 *coltw = smem + NG * kCols * R + grp * (kCols * K::COLTW_STRIDE);
-    const int lognc = a.logn - LOGR;
+    const int logn = LOGN_CT > 0 ? LOGN_CT : a.logn;
+    const int logp = LOGP_CT >= 0 ? LOGP_CT : a.logp;
+    const int tw_split = LOGN_CT > 0 ? (LOGN_CT + 1) / 2 : a.tw_split;
+    const int lognc = logn - LOGR;
     const uint32_t j0 = a.col0 + grp * kCols;
     const uint32_t j = j0 + c;
 
@@ -207,17 +213,17 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
         }
     }
     if (!FIRST) {
-        const uint32_t pmask = (1u << a.logp) - 1;
+        const uint32_t pmask = (1u << logp) - 1;
         // per-column factors W_{E p}^{e k} = W_N^{(e k) << (logn - LOGE - logp)}
-        const int sh_col = a.logn - C::LOGE - a.logp;
+        const int sh_col = logn - C::LOGE - logp;
         for (int i = lt; i < kCols * E; i += kCols * T) {
             const int cc = i >> C::LOGE, ee = i & (E - 1);
             const uint32_t kk = (j0 + cc) & pmask;
-            coltw[cc * K::COLTW_STRIDE + ee] = twiddle_2level(a.tw_lo, a.tw_hi, (kk * ee) << sh_col, a.tw_split);
+            coltw[cc * K::COLTW_STRIDE + ee] = twiddle_2level(a.tw_lo, a.tw_hi, (kk * ee) << sh_col, tw_split);
         }
         // per-thread factor W_{R p}^{t k}
         const uint32_t k = j & pmask;
-        const float2 w = twiddle_2level(a.tw_lo, a.tw_hi, (t * k) << (a.logn - LOGR - a.logp), a.tw_split);
+        const float2 w = twiddle_2level(a.tw_lo, a.tw_hi, (t * k) << (logn - LOGR - logp), tw_split);
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = cmul(v[e], cmul(w, coltw[c * K::COLTW_STRIDE + e]));
@@ -256,8 +262,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
             }
         }
     } else {
-        const uint32_t pmask = (1u << a.logp) - 1;
-        float2 *col = a.dst + ((uint64_t)(j >> a.logp) << (LOGR + a.logp)) + (j & pmask);
+        const uint32_t pmask = (1u << logp) - 1;
+        float2 *col = a.dst + ((uint64_t)(j >> logp) << (LOGR + logp)) + (j & pmask);
         if (a.out_re != 1.0f || a.out_im != 1.0f) {
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.out_re, v[e].y * a.out_im);
@@ -267,7 +273,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
 #pragma unroll
             for (int q = 0; q < (1 << LR); ++q) {
                 const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
-                st_stream(col + ((uint64_t)pos << a.logp), v[bb + q * NB]);
+                st_stream(col + ((uint64_t)pos << logp), v[bb + q * NB]);
             }
     }
 }

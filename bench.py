@@ -548,7 +548,9 @@ def main():
                        "placement": "out-of-place", "precision": args.precision, "window": args.window,
                        "form": ("single-pass" if logn <= 14 else
                                 "2-pass fused in one launch (intermediate in L2)" if launches_per_transform == 1
-                                else f"{round(launches_per_transform)}-pass"),
+                                else "3-pass: first pass, then passes 2-3 fused in one launch (intermediate in L2)"
+                                if logn > 20 and launches_per_transform == 2
+                                else f"{round(launches_per_transform)}-pass, one launch each"),
                        "l2": f"inputs ({8 * n * batch >> 20} MB) larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

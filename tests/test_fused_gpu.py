@@ -1,5 +1,6 @@
-"""GPU: the fused two-pass form (both global passes of N = 2^15 .. 2^20 in one
-persistent launch, intermediate read back from L2).
+"""GPU: the fused pass pairs (two global passes in one persistent launch,
+intermediate read back from L2): both passes of N = 2^15 .. 2^20, and the last
+two passes of N = 2^21 .. 2^26.
 
 The form runs the same tile arithmetic as the two-launch form, so its output
 must be bit-identical to it; both are also checked against FP64 at
@@ -117,3 +118,65 @@ def test_fused_in_place_falls_back(torch, oracle, lib_built, tmp_path, monkeypat
         torch.cuda.synchronize()
         assert ctx.launch_count() == 2
     assert oracle.rel_l2(d.cpu().numpy(), oracle.fft64(x, inverse=True)) <= TOL_REL_L2
+
+
+# ---- last two passes of a three-pass transform (radices 2^(L-16), 256, 256) ----
+
+@pytest.mark.parametrize("logn,batch", [(21, 3), (22, 2), (23, 1), (24, 1)])
+def test_fused_last_two_of_three_vs_fp64(torch, oracle, lib_built, tmp_path, monkeypatch, logn, batch):
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=340 + logn)
+    for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        (yf,), lf = _run(torch, x, d, True, tmp_path, monkeypatch)
+        (yp,), lp = _run(torch, x, d, False, tmp_path, monkeypatch)
+        assert lf == 2 and lp == 3  # first pass + the fused pair, against three launches
+        want = oracle.fft64(x, inverse=inv)
+        assert oracle.rel_l2(yf, want) <= TOL_REL_L2
+        assert oracle.rel_l2(yp, want) <= TOL_REL_L2
+
+
+def test_fused_last_two_of_three_in_place_and_repeated(torch, oracle, lib_built, tmp_path, monkeypatch):
+    import gbfft
+    from gbfft import signals
+    n, batch = 1 << 22, 3
+    _force(tmp_path, monkeypatch, 22, batch, True)
+    x = signals.uniform_c64(batch, n, seed=350)
+    want = oracle.fft64(x)
+    with gbfft.Context(0) as ctx:
+        d = torch.from_numpy(x).cuda()
+        ctx.c2c_device(d, d, n, batch, gbfft.FORWARD)  # in place: the first pass writes the workspace
+        torch.cuda.synchronize()
+        assert oracle.rel_l2(d.cpu().numpy(), want) <= TOL_REL_L2
+        dx = torch.from_numpy(x).cuda()
+        outs = []
+        for _ in range(3):  # the pair kernel clears its own counters
+            dy = torch.full_like(dx, float("nan"))
+            ctx.c2c_device(dx, dy, n, batch, gbfft.FORWARD)
+            torch.cuda.synchronize()
+            outs.append(dy.cpu().numpy())
+        assert ctx.launch_count() == 8
+    for y in outs:
+        assert np.array_equal(y, outs[0])
+    assert oracle.rel_l2(outs[0], want) <= TOL_REL_L2
+
+
+def test_fused_last_two_of_three_full_size_roundtrip(torch, lib_built):
+    """N = 2^26 (one transform, 512 MB) through the default plan: roundtrip and
+    Parseval (the FP64 oracle of a 2^26-point transform is too slow here)."""
+    import gbfft
+    from gbfft import signals
+    n = 1 << 26
+    x = signals.normal_c64_torch(1, n, seed=360)
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    with gbfft.Context(0) as ctx:
+        ctx.c2c_device(x, y, n, 1, gbfft.FORWARD)
+        ctx.c2c_device(y, z, n, 1, gbfft.INVERSE)
+        torch.cuda.synchronize()
+        assert ctx.launch_count() == 4
+    rt = (torch.linalg.vector_norm(z - x) / torch.linalg.vector_norm(x)).item()
+    assert rt < 1e-6
+    ex = torch.linalg.vector_norm(x.to(torch.complex128)).item() ** 2
+    ey = torch.linalg.vector_norm(y.to(torch.complex128)).item() ** 2 / n
+    assert abs(ey / ex - 1) < 1e-5

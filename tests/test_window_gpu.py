@@ -74,3 +74,25 @@ def test_window_limits(wctx):
     wctx.set_window(gbfft.WINDOW_NONE)
     x = np.ones((1, 8), np.complex64)
     assert np.allclose(wctx.c2c_host(x, gbfft.FORWARD)[0], [8, 0, 0, 0, 0, 0, 0, 0], atol=1e-6)
+
+
+@pytest.mark.parametrize("logn,batch", [(15, 6), (16, 40), (18, 3), (20, 2)])
+def test_hann_fused_two_pass_device_entry(lib_built, oracle, logn, batch):
+    """Out of place on the device, N = 2^15..2^20 runs the fused two-pass
+    launch; the window is applied by its first-pass tiles."""
+    torch = pytest.importorskip("torch")
+    import gbfft
+    from gbfft import signals
+    n = 1 << logn
+    x = signals.normal_c64(batch, n, seed=95 + logn)
+    xw = x.astype(np.complex128) * signals.hann_window(n).astype(np.float64)[None, :]
+    dx = torch.from_numpy(x).cuda()
+    dy = torch.empty_like(dx)
+    with gbfft.Context(0) as ctx:
+        ctx.set_window(gbfft.WINDOW_HANN)
+        for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+            l0 = ctx.launch_count()
+            ctx.c2c_device(dx, dy, n, batch, d)
+            torch.cuda.synchronize()
+            assert ctx.launch_count() - l0 == 1  # the fused form ran
+            assert oracle.rel_l2(dy.cpu().numpy(), oracle.fft64(xw, inverse=inv)) <= TOL, (logn, inv)

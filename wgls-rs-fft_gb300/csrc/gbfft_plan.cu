@@ -73,12 +73,14 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
     }
     const bool tc = precision != GBFFT_PREC_FP32;
     const int top = tc ? 9 : 10;
+    FusedDesc fd;
+    // three passes (L - 16, 8, 8) with the last two fused: the default where it exists
+    if (!tc && fused3_kernel_info(logn, fd)) c.push_back(PlanVariant{10, false, true});
     for (int m = top; m >= 7; --m) {
         const std::vector<int> parts = split_passes(logn, m);
         bool dup = false;
         for (const PlanVariant &v : c) dup |= split_passes(logn, v.max_logr) == parts;
         if (dup || parts[0] < 5) continue;
-        Fused2Desc fd;
         if (!tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd))
             c.push_back(PlanVariant{m, false, true});
         c.push_back(PlanVariant{m, false});
@@ -116,6 +118,8 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         p.needs_workspace = true;
         // the split form's radix-2^10 tile would not fit in shared memory
         std::vector<int> parts = split_passes(logn, tc ? std::min(9, v.max_logr) : v.max_logr);
+        const bool fused3 = v.fused && !tc && fused3_kernel_info(logn, p.fused);
+        if (fused3) parts = {logn - 16, 8, 8};
         int logp = 0;
         for (size_t i = 0; i < parts.size(); ++i) {
             PassDesc d;
@@ -135,8 +139,8 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
             p.passes.push_back(d);
         }
         p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
-        if (v.fused && !tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], p.fused)) {
-            if ((e = fused2_prepare(p.fused)) != cudaSuccess) {
+        if (fused3 || (v.fused && !tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], p.fused))) {
+            if ((e = fused_prepare(p.fused)) != cudaSuccess) {
                 why = cudaGetErrorString(e);
                 return GBFFT_ERR_CUDA;
             }
@@ -174,8 +178,14 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
     launches = 0;
     if (batch == 0) return GBFFT_OK;
     cudaError_t e;
-    if (p.has_fused && ctr && (const void *)in != (const void *)out && batch <= 0x7fffffffull) {
-        const size_t want = (2 + (size_t)batch) * sizeof(uint32_t);
+    // Fused pass pair: both passes of a two-pass transform (out of place
+    // only: its first pass writes into `out` while other tiles still read
+    // `in`), or the last two of three after the first pass into the workspace.
+    const bool pair3 = p.has_fused && p.passes.size() == 3;
+    const bool pair2 = p.has_fused && p.passes.size() == 2 && (const void *)in != (const void *)out;
+    const uint64_t ngroups = batch * p.fused.groups_per_transform;
+    if ((pair2 || pair3) && ctr && ngroups <= 0x7fffffffull) {
+        const size_t want = (2 + (size_t)ngroups) * sizeof(uint32_t);
         if (ctr->bytes < want) {
             int st = ctr->ensure(want, why);
             if (st != GBFFT_OK) return st;
@@ -187,15 +197,31 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
         }
         const bool inv = direction == GBFFT_INVERSE;
         const float scale = inv ? ldexpf(1.0f, -p.logn) : 1.0f;
-        const PassDesc &d1 = p.passes[0], &d2 = p.passes[1];
-        e = fused2_launch(p.fused, in, out, batch, p.logn, p.tw + d1.sub_tw_offset, p.tw + d2.sub_tw_offset,
-                          p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset, p.tw_split, inv ? -1.0f : 1.0f, scale,
-                          inv ? -scale : 1.0f, ops, (uint32_t *)ctr->ptr, err, p.sms, stream);
+        const float2 *pair_in = in;
+        const size_t a = pair3 ? 1 : 0;  // index of the pair's first pass
+        if (pair3) {
+            int st = ws.ensure(((size_t)batch << p.logn) * sizeof(float2), why);
+            if (st != GBFFT_OK) return st;
+            const PassDesc &d0 = p.passes[0];
+            e = pass_launch(d0, in, (float2 *)ws.ptr, batch, p.logn, p.tw + d0.sub_tw_offset, p.tw + p.tw_lo_offset,
+                            p.tw + p.tw_hi_offset, p.tw_split, inv ? -1.0f : 1.0f, 1.0f, 1.0f, stream, false, p.sms,
+                            ops);
+            if (e != cudaSuccess) {
+                why = cudaGetErrorString(e);
+                return GBFFT_ERR_CUDA;
+            }
+            ++launches;
+            pair_in = (const float2 *)ws.ptr;
+        }
+        e = fused_launch(p.fused, pair_in, out, batch, p.tw + p.passes[a].sub_tw_offset,
+                         p.tw + p.passes[a + 1].sub_tw_offset, p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset,
+                         (inv && !pair3) ? -1.0f : 1.0f, scale, inv ? -scale : 1.0f,
+                         pair3 ? LoadOps{nullptr, 0u, 0.f, 0u} : ops, (uint32_t *)ctr->ptr, err, p.sms, stream);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;
         }
-        launches = 1;
+        ++launches;
         return GBFFT_OK;
     }
     if (!p.multipass) {

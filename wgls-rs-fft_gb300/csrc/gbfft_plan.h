@@ -36,19 +36,24 @@ struct PassDesc {
     bool tc = false;                    // radix-16 butterflies on the tensor cores
 };
 
-// Both passes of a two-pass transform in one persistent launch whose queue
-// alternates first-pass tiles of transform b with second-pass tiles of
-// transform b - LAG, so that the intermediate is read back from L2
-// (fft_fused2.cu).
-struct Fused2Desc {
+// Two consecutive passes in one persistent launch whose queue alternates the
+// first pass's tiles of group x with the second pass's tiles of group x - LAG,
+// so that the intermediate is read back from L2 (fft_fused.cuh): both passes
+// of a two-pass transform, or the last two of a three-pass one.
+struct FusedDesc {
     const void *fn = nullptr;
     int threads = 0;
     size_t smem = 0;
-    int logr1 = 0, logr2 = 0;
+    int logra = 0, logrb = 0;  // radices of the two passes
+    int logpa = 0;             // product of the radices before them (0: the pair starts the transform)
+    int logn = 0;
+    uint32_t groups_per_transform = 1;
+    uint32_t tiles_per_group = 0;  // of each pass
+    uint64_t group_samples = 0;
     int ctas_per_sm = 0;
 };
 // Upper bound on the intermediates in flight between the two passes (bytes).
-constexpr uint64_t kFused2WindowBytes = 48ull << 20;
+constexpr uint64_t kFusedWindowBytes = 48ull << 20;
 
 // The tunable choices of a plan: largest global-pass radix (multi-pass split),
 // whether kernels run as persistent tile loops with L2 prefetch, and whether a
@@ -77,8 +82,8 @@ struct Plan {
     bool needs_workspace = false;
     RowsKernelInfo rows;
     std::vector<PassDesc> passes;
-    bool has_fused = false;  // variant.fused and a kernel exists for the two radices
-    Fused2Desc fused;
+    bool has_fused = false;  // variant.fused and a kernel exists for the split
+    FusedDesc fused;
     // twiddle table (device): rows sub-pass tables, or for multi-pass the
     // per-pass sub-pass tables followed by the two-level W_N table.
     float2 *tw = nullptr;
@@ -105,14 +110,14 @@ cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uin
 cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
 constexpr size_t kTcGtabBytes = 4 * 2048;
 
-// fft_fused2.cu
-bool fused2_kernel_info(int logr1, int logr2, Fused2Desc &d);
-cudaError_t fused2_prepare(Fused2Desc &d);
-uint32_t fused2_lag(const Fused2Desc &d, int logn, uint64_t batch, int sms);
-cudaError_t fused2_launch(const Fused2Desc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
-                          const float2 *tw1, const float2 *tw2, const float2 *tw_lo, const float2 *tw_hi,
-                          int tw_split, float in_im, float out_re, float out_im, LoadOps ops, uint32_t *ctr,
-                          uint32_t *err, int sms, cudaStream_t stream);
+// fft_fused2.cu, fft_fused3.cu
+bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d);
+bool fused3_kernel_info(int logn, FusedDesc &d);  // passes 2-3 of (logn - 16, 8, 8)
+cudaError_t fused_prepare(FusedDesc &d);
+uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms);
+cudaError_t fused_launch(const FusedDesc &d, const float2 *in, float2 *out, uint64_t batch, const float2 *tw_a,
+                         const float2 *tw_b, const float2 *tw_lo, const float2 *tw_hi, float in_im, float out_re,
+                         float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream);
 
 // log2 radices (each <= max_logr) of the global passes for a multi-pass
 // transform of 2^logn.

@@ -1,6 +1,7 @@
 """GPU: the autotuner and every plan variant it chooses between.
 
-Each variant (global-pass split cap, plain or persistent tile-loop kernels) is
+Each variant (global-pass split cap, plain or persistent tile-loop kernels,
+samples -- hence transforms -- per CTA of the single-pass kernel) is
 forced through the documented on-disk cache (GBFFT_AUTOTUNE_CACHE) and checked
 against FP64 at rel-L2 <= 2e-6; the tuner itself must return a positive time,
 keep results correct and append its choice to the cache file."""
@@ -14,10 +15,10 @@ pytestmark = pytest.mark.gpu
 TOL_REL_L2 = 2e-6
 
 
-def _cache_line(logn, batch, direction, max_logr, persistent, precision=0):
+def _cache_line(logn, batch, direction, max_logr, persistent, precision=0, tile=0):
     return json.dumps({"arch": "sm_103", "logn": logn, "precision": precision, "direction": direction,
                        "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": persistent,
-                       "fused": 0, "seconds": 1.0})
+                       "fused": 0, "tile": tile, "seconds": 1.0})
 
 
 @pytest.mark.parametrize("logn,batch,max_logr,persistent", [
@@ -67,3 +68,22 @@ def test_autotune_on_first_use(monkeypatch, oracle, lib_built):
         x = signals.uniform_c64(8, 1 << 17, seed=81)
         y = ctx.c2c_host(x, gbfft.INVERSE)
         assert oracle.rel_l2(y, oracle.fft64(x, inverse=True)) <= TOL_REL_L2
+
+
+@pytest.mark.parametrize("logn", [6, 8, 10, 11])
+@pytest.mark.parametrize("tile,persistent", [(11, 0), (13, 0), (13, 1)])
+def test_forced_transforms_per_cta(tmp_path, monkeypatch, oracle, lib_built, logn, tile, persistent):
+    """Single-pass kernels moving 2^11 or 2^13 samples per CTA (half or twice
+    the default number of transforms per CTA), batch not a multiple of it."""
+    import gbfft
+    from gbfft import signals
+    batch = (1 << (14 - logn)) + 3
+    cache = tmp_path / "tune.jsonl"
+    cache.write_text("\n".join(_cache_line(logn, batch, d, 10, persistent, tile=tile)
+                               for d in (gbfft.FORWARD, gbfft.INVERSE)) + "\n")
+    monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+    x = signals.normal_c64(batch, 1 << logn, seed=500 + logn + tile)
+    with gbfft.Context(0) as ctx:
+        for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+            y = ctx.c2c_host(x, d)
+            assert oracle.rel_l2(y, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2

@@ -32,7 +32,7 @@ def _force(tmp_path, monkeypatch, logn, batch, fused, max_logr=10):
     for d in (gbfft.FORWARD, gbfft.INVERSE):
         lines.append(json.dumps({"arch": "sm_103", "logn": logn, "precision": 0, "direction": d,
                                  "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": 0,
-                                 "fused": int(fused), "seconds": 1.0}))
+                                 "fused": int(fused), "tile": 0, "seconds": 1.0}))
     cache = tmp_path / f"tune_{int(fused)}.jsonl"
     cache.write_text("\n".join(lines) + "\n")
     monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))

@@ -4,8 +4,8 @@
 // dispatched by src/lib.rs:582-628), each of which round-trips all 8*N*B bytes
 // through memory.
 //
-// One CTA transforms G whole rows (G*N = 4096 samples for N <= 4096, one row
-// above):
+// One CTA transforms G whole rows (G*N = 4096 samples for N <= 4096 -- or
+// 2048 / 8192, the tuner's alternatives for N = 2^6 .. 2^11 -- one row above):
 //   * each thread owns E = 16 samples of one row (T = N/E threads per row) and
 //     loads them straight from HBM into registers -- sample t + T*e, so a warp
 //     reads 256 contiguous bytes per load instruction;
@@ -23,22 +23,25 @@
 
 namespace gbfft {
 
-template <int LOGN>
+// LOGS: log2 of the samples one CTA moves (2^12 by default; 2^11 and 2^13 are
+// the autotuner's "transforms per CTA" alternatives for N <= 2^11).
+template <int LOGN, int LOGS = 12>
 struct RowsCfg : SubCfg<LOGN> {
     using S = SubCfg<LOGN>;
-    static constexpr int G_BY_SAMPLES = S::N >= 4096 ? 1 : 4096 / S::N;
-    static constexpr int G_BY_THREADS = S::T >= 256 ? 1 : 256 / S::T;
+    static constexpr int TILE = 1 << LOGS;
+    static constexpr int G_BY_SAMPLES = S::N >= TILE ? 1 : TILE / S::N;
+    static constexpr int G_BY_THREADS = S::T >= TILE / 16 ? 1 : (TILE / 16) / S::T;
     static constexpr int G = G_BY_SAMPLES < G_BY_THREADS ? G_BY_SAMPLES : G_BY_THREADS;
     static constexpr int THREADS = G * S::T;
-    static constexpr int MINB = THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 4);
+    static constexpr int MINB = THREADS >= 1024 ? 1 : 1024 / THREADS;  // 64 registers a thread
     static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * S::N * sizeof(float2) : 0;
 };
 
-template <int LOGN>
-__global__ void __launch_bounds__(RowsCfg<LOGN>::THREADS, RowsCfg<LOGN>::MINB)
+template <int LOGN, int LOGS>
+__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS>::THREADS, RowsCfg<LOGN, LOGS>::MINB)
 fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                 float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
-    using C = RowsCfg<LOGN>;
+    using C = RowsCfg<LOGN, LOGS>;
     extern __shared__ float2 smem_rows[];
     auto ref = [&](int g) {
         const uint64_t row = (uint64_t)blockIdx.x * C::G + g;
@@ -53,11 +56,11 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
 // blockIdx.x, +gridDim.x, ... and, before computing a tile, asks L2 for the
 // next one (one 128-byte line per thread), so the HBM fetch of tile i+1
 // overlaps the shared-memory sub-passes of tile i.
-template <int LOGN>
-__global__ void __launch_bounds__(RowsCfg<LOGN>::THREADS, RowsCfg<LOGN>::MINB)
+template <int LOGN, int LOGS>
+__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS>::THREADS, RowsCfg<LOGN, LOGS>::MINB)
 fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                            float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
-    using C = RowsCfg<LOGN>;
+    using C = RowsCfg<LOGN, LOGS>;
     extern __shared__ float2 smem_rows[];
     constexpr uint32_t kTileSamples = C::G * C::N;
     constexpr uint32_t kLines = kTileSamples * sizeof(float2) / 128;
@@ -83,11 +86,11 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
 // host side
 // ---------------------------------------------------------------------------
 
-template <int LOGN>
+template <int LOGN, int LOGS = 12>
 static void rows_describe(RowsKernelInfo &k) {
-    using C = RowsCfg<LOGN>;
-    k.fn = (const void *)fft_rows_kernel<LOGN>;
-    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN>;
+    using C = RowsCfg<LOGN, LOGS>;
+    k.fn = (const void *)fft_rows_kernel<LOGN, LOGS>;
+    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN, LOGS>;
     k.threads = C::THREADS;
     k.transforms_per_cta = C::G;
     k.smem = C::SMEM;
@@ -95,7 +98,20 @@ static void rows_describe(RowsKernelInfo &k) {
     k.tw_entries = C::tw_entries();
 }
 
-bool rows_kernel_info(int logn, RowsKernelInfo &k) {
+bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs) {
+    if (logs == 11 || logs == 13) {  // other tile sizes for the sizes that batch transforms in a CTA
+        switch (logn) {
+#define GBFFT_ROWS_TILE(L)                                              \
+    case L:                                                            \
+        if (logs == 11) rows_describe<L, 11>(k); else rows_describe<L, 13>(k); \
+        return true;
+            GBFFT_ROWS_TILE(6) GBFFT_ROWS_TILE(7) GBFFT_ROWS_TILE(8) GBFFT_ROWS_TILE(9)
+            GBFFT_ROWS_TILE(10) GBFFT_ROWS_TILE(11)
+#undef GBFFT_ROWS_TILE
+            default: return false;
+        }
+    }
+    if (logs != 12) return false;
     switch (logn) {
 #define GBFFT_ROWS_CASE(L) \
     case L: rows_describe<L>(k); return true;

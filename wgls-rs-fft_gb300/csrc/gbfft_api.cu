@@ -270,9 +270,10 @@ int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *
         const double s = (double)ms * 1e-3 / reps;
         if (ctx->tune_verbose)
             fprintf(stderr,
-                    "gbfft autotune N=2^%d batch=%llu dir=%d prec=%d max_logr=%d persistent=%d fused=%d: %.3f us\n",
+                    "gbfft autotune N=2^%d batch=%llu dir=%d prec=%d max_logr=%d persistent=%d fused=%d "
+                    "tile=%d: %.3f us\n",
                     logn, (unsigned long long)batch, direction, ctx->precision, v.max_logr, v.persistent ? 1 : 0,
-                    v.fused ? 1 : 0,
+                    v.fused ? 1 : 0, v.tile,
                     s * 1e6);
         if (s < best) {
             best = s;
@@ -288,9 +289,9 @@ int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *
         if (f) {
             fprintf(f,
                     "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
-                    "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"seconds\": %.9g}\n",
+                    "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"tile\": %d, \"seconds\": %.9g}\n",
                     logn, ctx->precision, direction, log2floor(batch), best_v.max_logr, best_v.persistent ? 1 : 0,
-                    best_v.fused ? 1 : 0,
+                    best_v.fused ? 1 : 0, best_v.tile,
                     best);
             fclose(f);
         }
@@ -303,13 +304,13 @@ void load_tune_cache(gbfft_ctx *ctx) {
     if (!f) return;
     char line[512];
     while (fgets(line, sizeof line, f)) {
-        int logn, prec, dir, blog, mlr, pers, fused;
+        int logn, prec, dir, blog, mlr, pers, fused, tile;
         double sec;
         if (sscanf(line,
                    "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
-                   "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"seconds\": %lf}",
-                   &logn, &prec, &dir, &blog, &mlr, &pers, &fused, &sec) == 8)
-            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] = PlanVariant{mlr, pers != 0, fused != 0};
+                   "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"tile\": %d, \"seconds\": %lf}",
+                   &logn, &prec, &dir, &blog, &mlr, &pers, &fused, &tile, &sec) == 9)
+            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] = PlanVariant{mlr, pers != 0, fused != 0, tile};
     }
     fclose(f);
 }

@@ -65,10 +65,15 @@ uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t of
 std::vector<PlanVariant> plan_candidates(int logn, int precision) {
     std::vector<PlanVariant> c;
     if (logn <= kRowsMaxLogN) {
-        // one CTA per SM leaves no other CTA to overlap with: prefetch helps
+        // 2^11 samples per CTA (128 threads, 8 CTAs per SM) measured fastest
+        // where a transform fits (N = 2^6 .. 2^11); one CTA per SM leaves no
+        // other CTA to overlap with at 2^14, so prefetch helps there
+        RowsKernelInfo ri;
+        if (rows_kernel_info(logn, ri, 11)) c.push_back(PlanVariant{10, false, false, 11});
         const bool big = logn >= 14;
         c.push_back(PlanVariant{10, big});
         c.push_back(PlanVariant{10, !big});
+        if (rows_kernel_info(logn, ri, 13)) c.push_back(PlanVariant{10, false, false, 13});
         return c;
     }
     const bool tc = precision != GBFFT_PREC_FP32;
@@ -103,7 +108,7 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         return GBFFT_ERR_UNSUPPORTED;
     }
     if (logn <= kRowsMaxLogN) {
-        if (!rows_kernel_info(logn, p.rows)) {
+        if (!rows_kernel_info(logn, p.rows, v.tile ? v.tile : 12)) {
             why = "no single-pass kernel";
             return GBFFT_ERR_UNSUPPORTED;
         }

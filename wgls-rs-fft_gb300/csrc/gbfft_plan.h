@@ -56,19 +56,22 @@ struct FusedDesc {
 constexpr uint64_t kFusedWindowBytes = 48ull << 20;
 
 // The tunable choices of a plan: largest global-pass radix (multi-pass split),
-// whether kernels run as persistent tile loops with L2 prefetch, and whether a
-// two-pass transform runs as one launch with an L2-resident intermediate.
+// whether kernels run as persistent tile loops with L2 prefetch, whether pass
+// pairs run as one launch with an L2-resident intermediate, and (single pass)
+// how many transforms a CTA takes.
 struct PlanVariant {
     int max_logr = 10;
     bool persistent = false;
     bool fused = false;
+    int tile = 0;  // single pass: log2 of the samples a CTA moves (0: 2^12), i.e. transforms per CTA
     bool operator<(const PlanVariant &o) const {
         if (max_logr != o.max_logr) return max_logr < o.max_logr;
         if (persistent != o.persistent) return persistent < o.persistent;
-        return fused < o.fused;
+        if (fused != o.fused) return fused < o.fused;
+        return tile < o.tile;
     }
     bool operator==(const PlanVariant &o) const {
-        return max_logr == o.max_logr && persistent == o.persistent && fused == o.fused;
+        return max_logr == o.max_logr && persistent == o.persistent && fused == o.fused && tile == o.tile;
     }
 };
 

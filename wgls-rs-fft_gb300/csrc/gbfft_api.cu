@@ -55,6 +55,7 @@ struct gbfft_ctx {
     size_t hstage_bytes = 0;
     uint64_t launches = 0;
     int precision = GBFFT_PREC_FP32;
+    size_t host_chunk = (size_t)32 << 20;  // bytes of a host batch per pipelined copy (GBFFT_HOST_CHUNK_BYTES)
 };
 
 namespace {
@@ -377,6 +378,10 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
         return GBFFT_ERR_CUDA;
     if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_OUT_OF_MEMORY;
     if (cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_CUDA;
+    if (const char *c = getenv("GBFFT_HOST_CHUNK_BYTES")) {
+        const long long v = atoll(c);
+        if (v >= (1 << 16)) ctx->host_chunk = (size_t)v;
+    }
     if (const char *c = getenv("GBFFT_AUTOTUNE_CACHE")) {
         ctx->tune_cache = c;
         load_tune_cache(ctx.get());
@@ -475,7 +480,7 @@ static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t
     // H2D -> transform -> D2H over three streams so the two copy directions and
     // the kernels overlap.
     const size_t row_bytes = (size_t)n * sizeof(float2);
-    const size_t chunk_target = (size_t)32 << 20;
+    const size_t chunk_target = ctx->host_chunk;
     uint64_t rows_per_chunk = row_bytes >= chunk_target ? 1 : chunk_target / row_bytes;
     if (log2u(n) > kRowsMaxLogN) rows_per_chunk = batch;  // multi-pass shares one workspace: no overlap
     uint64_t done = 0;

@@ -156,7 +156,7 @@ struct PassArgs {
     float in_im;          // -1: conjugate the input (first pass of an inverse)
     float out_re, out_im; // output scale; later passes only (a first pass never scales)
     bool coherent_load;  // input written earlier in the same kernel: bypass L1
-    bool keep_l2 = false;  // first pass: output is read again soon, store it with normal L2 priority
+    bool keep_l2 = false;  // output is read again soon (fused pairs): store it with normal L2 priority
     uint32_t row;        // batch index of the transform (noise stream)
     LoadOps ops;         // first pass: noise / window applied on load
 };
@@ -268,13 +268,23 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
 #pragma unroll
             for (int e = 0; e < E; ++e) v[e] = make_float2(v[e].x * a.out_re, v[e].y * a.out_im);
         }
+        if (a.keep_l2) {
 #pragma unroll
-        for (int bb = 0; bb < NB; ++bb)
+            for (int bb = 0; bb < NB; ++bb)
 #pragma unroll
-            for (int q = 0; q < (1 << LR); ++q) {
-                const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
-                st_stream(col + ((uint64_t)pos << logp), v[bb + q * NB]);
-            }
+                for (int q = 0; q < (1 << LR); ++q) {
+                    const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
+                    __stcg(col + ((uint64_t)pos << logp), v[bb + q * NB]);
+                }
+        } else {
+#pragma unroll
+            for (int bb = 0; bb < NB; ++bb)
+#pragma unroll
+                for (int q = 0; q < (1 << LR); ++q) {
+                    const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
+                    st_stream(col + ((uint64_t)pos << logp), v[bb + q * NB]);
+                }
+        }
     }
 }
 

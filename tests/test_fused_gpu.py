@@ -180,3 +180,16 @@ def test_fused_last_two_of_three_full_size_roundtrip(torch, lib_built):
     ex = torch.linalg.vector_norm(x.to(torch.complex128)).item() ** 2
     ey = torch.linalg.vector_norm(y.to(torch.complex128)).item() ** 2 / n
     assert abs(ey / ex - 1) < 1e-5
+
+
+@pytest.mark.parametrize("logn,batch", [(13, 5), (13, 64), (14, 3), (14, 33)])
+def test_fused_radix128_pair_for_single_pass_sizes(torch, oracle, lib_built, tmp_path, monkeypatch, logn, batch):
+    """N = 2^13, 2^14 as a fused two-pass transform of radix-128 tiles (an
+    autotuner candidate beside the single-pass kernels)."""
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=370 + logn)
+    for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        (yf,), lf = _run(torch, x, d, True, tmp_path, monkeypatch)
+        assert lf == 1
+        assert oracle.rel_l2(yf, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2

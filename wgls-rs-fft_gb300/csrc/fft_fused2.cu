@@ -12,6 +12,8 @@ namespace gbfft {
 bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d) {
 #define GBFFT_F2(A, B, T) \
     if (logr1 == A && logr2 == B) { fused_describe<A, B, T, A + B, 0>(d); return true; }
+    GBFFT_F2(7, 6, 128)
+    GBFFT_F2(7, 7, 128)
     GBFFT_F2(8, 7, 256)
     GBFFT_F2(8, 8, 256)
     GBFFT_F2(9, 8, 512)

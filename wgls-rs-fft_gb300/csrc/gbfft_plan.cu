@@ -74,6 +74,8 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         c.push_back(PlanVariant{10, big});
         c.push_back(PlanVariant{10, !big});
         if (rows_kernel_info(logn, ri, 13)) c.push_back(PlanVariant{10, false, false, 13});
+        FusedDesc fd;
+        if (precision == GBFFT_PREC_FP32 && fused2_kernel_info(7, logn - 7, fd)) c.push_back(PlanVariant{10, false, true});
         return c;
     }
     const bool tc = precision != GBFFT_PREC_FP32;
@@ -107,7 +109,10 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         why = "the tensor-core split form covers N >= 2^15 (multi-pass transforms)";
         return GBFFT_ERR_UNSUPPORTED;
     }
-    if (logn <= kRowsMaxLogN) {
+    // N = 2^13, 2^14 may also run as a fused two-pass transform of radix-128
+    // tiles (a tuner candidate)
+    const bool small_fused = v.fused && !tc && (logn == 13 || logn == 14);
+    if (logn <= kRowsMaxLogN && !small_fused) {
         if (!rows_kernel_info(logn, p.rows, v.tile ? v.tile : 12)) {
             why = "no single-pass kernel";
             return GBFFT_ERR_UNSUPPORTED;
@@ -123,6 +128,7 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         p.needs_workspace = true;
         // the split form's radix-2^10 tile would not fit in shared memory
         std::vector<int> parts = split_passes(logn, tc ? std::min(9, v.max_logr) : v.max_logr);
+        if (small_fused) parts = {7, logn - 7};
         const bool fused3 = v.fused && !tc && fused3_kernel_info(logn, p.fused);
         if (fused3) parts = {logn - 16, 8, 8};
         int logp = 0;

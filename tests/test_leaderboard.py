@@ -1,0 +1,67 @@
+"""The rivalry leaderboard (gbfft.leaderboard), mirroring the reference's
+examples/rivalry_leaderboard.rs: its batch rule and tests (:147-202), its
+benchmark input (src/benchmark.rs:112-122), table and validation at 1e-3;
+the GPU test runs the registered rivals."""
+import numpy as np
+import pytest
+
+
+def test_choose_batch_size_matches_reference_rule(lib_built):
+    from gbfft import leaderboard as lb
+    assert lb.choose_batch_size(256) == 1024 and lb.choose_batch_size(1024) == 1024
+    assert lb.choose_batch_size(16384) == 256 and lb.choose_batch_size(65536) == 64
+    assert lb.choose_batch_size(262_144) == 16 and lb.choose_batch_size(1_048_576) == 1
+    for n in (1, 2, 256, 1024, 16384, 65536, 262_144, 1_048_576, 1 << 26):
+        b = lb.choose_batch_size(n)
+        assert b >= 1 and (n * b <= lb.MAX_TOTAL_SAMPLES or b == 1)
+
+
+def test_pipeline_input_and_validation(lib_built):
+    from gbfft import leaderboard as lb
+    rows = lb.pipeline_input(8, 2)
+    t = np.arange(8, dtype=np.float32) / np.float32(8)
+    assert rows[0].dtype == np.complex64 and len(rows) == 2
+    assert np.allclose(rows[1].real, t * 0.001) and np.allclose(rows[1].imag, np.sin(2 * np.pi * t) * 0.001)
+    ref = lb.baseline_fft(rows)
+    assert lb.validate([r.astype(np.complex64) for r in ref], ref) is None
+    bad = [ref[0] + 2e-3, ref[1]]
+    assert lb.validate(bad, ref) == pytest.approx(2e-3, rel=1e-6)
+
+
+def test_run_rival_and_table_with_a_cpu_rival(lib_built):
+    from gbfft import leaderboard as lb
+    from gbfft.gpu_fft import FftExecutor
+
+    class NumpyRival(FftExecutor):
+        def name(self):
+            return "numpy f32"
+
+        def fft(self, inputs):
+            return list(np.fft.fft(np.stack(inputs), axis=1).astype(np.complex64))
+
+    ticks = iter([0.0, 0.5])
+    r = lb.run_rival(NumpyRival(), 256, 4, clock=lambda: next(ticks))
+    assert r.status == "PASS" and r.batch == 4
+    assert r.msamples_per_sec == pytest.approx(256 * 4 / 0.05 / 1e6)
+    assert r.gflops == pytest.approx(5 * 256 * 4 * 8 / 0.05 / 1e9)
+    table = lb.format_table(256, [r, lb.Result("broken", 4, None, None, "UNSUPPORTED")])
+    assert "--- N = 256 ---" in table and "numpy f32" in table and "ERROR" in table and "UNSUPPORTED" in table
+
+
+@pytest.mark.gpu
+def test_leaderboard_rivals_pass_on_gpu(lib_built, capsys):
+    import gbfft
+    from gbfft import leaderboard as lb
+    rivals = lb.default_rivals()
+    names = [r.name() for r in rivals]
+    assert any("GB300" in n for n in names) and any("cuFFT" in n for n in names)
+    for n in (1024, 65536):
+        results = [lb.run_rival(r, n, lb.choose_batch_size(n)) for r in rivals]
+        for res in results:
+            if res.name.startswith("GB300 split") and n < (1 << 15):
+                assert res.status == gbfft.status_string(gbfft.ERR_UNSUPPORTED)
+            else:
+                assert res.status == "PASS", (n, res)
+                assert res.msamples_per_sec > 0
+    assert lb.main(["--sizes", "256"]) == 0
+    assert "RIVALRY LEADERBOARD" in capsys.readouterr().out

@@ -188,6 +188,21 @@ def test_gpufft_mirror(lib_built):
     assert maxdiff(np.stack(rec), np.stack(x)) < 1e-5
     assert f.fft([]) == []
     assert f.benchmark_gpu_only(256, 64, warmup=1, iters=3) > 0
+    # the reference's errors and messages on both routes (equal lengths go
+    # through the contiguous entry, unequal ones through the row entry)
+    with pytest.raises(gbfft.GbfftError) as e:
+        f.fft([np.zeros(6, np.complex64)] * 3)
+    assert e.value.status == gbfft.ERR_INVALID_SIZE
+    assert "Transform length must be a non-zero power of two" in str(e.value)
+    with pytest.raises(gbfft.GbfftError) as e:
+        f.fft([np.zeros(0, np.complex64)])
+    assert e.value.status == gbfft.ERR_INVALID_SIZE
+    with pytest.raises(gbfft.GbfftError) as e:
+        f.ifft([np.zeros(8, np.complex64), np.zeros(16, np.complex64)])
+    assert e.value.status == gbfft.ERR_LENGTH_MISMATCH
+    assert "All input vectors in a batch must have the same length" in str(e.value)
+    rows = f.fft([r.astype(np.complex128) for r in x])  # any complex dtype in, complex64 rows out
+    assert len(rows) == 2 and rows[0].dtype == np.complex64 and maxdiff(np.stack(rows), np.stack(spec)) == 0
 
 
 # ---- device-resident entry point ------------------------------------------------

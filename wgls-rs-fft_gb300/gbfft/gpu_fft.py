@@ -66,6 +66,14 @@ class GpuFft(FftExecutor):
     def _run(self, inputs, direction):
         if len(inputs) == 0:  # src/lib.rs:522-524
             return []
+        n = len(inputs[0])
+        if n <= 2048 and all(len(r) == n for r in inputs):
+            # many short rows: marshalling each row costs more than one extra
+            # copy, so stack them (at C speed) into one contiguous batch for the
+            # contiguous entry, which checks the length the same way
+            out = self._ctx.c2c_host(np.stack(inputs).astype(np.complex64, copy=False), direction)
+            return list(out)
+        # unequal lengths: the row entry reports the reference's error, in its order
         return self._ctx.c2c_host_rows(inputs, direction)
 
     def fft(self, inputs):

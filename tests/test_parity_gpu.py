@@ -278,3 +278,37 @@ def test_large_n_sampled(gpu_ctx, oracle, torch_cuda, logn, batch):
     torch.cuda.synchronize()
     xs = x.cpu().numpy()
     assert oracle.rel_l2(y.cpu().numpy(), oracle.fft64(xs)) <= TOL_REL_L2
+
+
+# ---- largest transforms ------------------------------------------------------------
+
+@pytest.mark.parametrize("logn", [27, 28, 30])
+def test_largest_transforms_roundtrip(gpu_ctx, torch_cuda, logn):
+    """N = 2^27, 2^28 and the largest supported 2^30 (8 GB per buffer) on the
+    device entry: forward then inverse gives back the input, Parseval holds,
+    and one output bin matches a direct float64 sum over the input.  2^31 is
+    refused."""
+    import gbfft
+    torch = torch_cuda
+    n = 1 << logn
+    g = torch.Generator(device="cuda").manual_seed(logn)
+    x = torch.randn(n, dtype=torch.complex64, device="cuda", generator=g)
+    y = torch.empty_like(x)
+    gpu_ctx.c2c_device(x, y, n, 1, gbfft.FORWARD)
+    ex = torch.linalg.vector_norm(x.to(torch.complex128)).item() ** 2
+    ey = torch.linalg.vector_norm(y.to(torch.complex128)).item() ** 2 / n
+    assert abs(ey / ex - 1) < 1e-5
+    k = 12345  # X[k] = sum_j x[j] e^{-2 pi i j k / N}, summed in float64 on the device
+    j = torch.arange(n, device="cuda", dtype=torch.float64)
+    ang = -2 * np.pi * ((j * k) % n) / n
+    xk = (x.to(torch.complex128) * torch.polar(torch.ones_like(ang), ang)).sum().item()
+    assert abs(y[k].item() - xk) <= 2e-6 * (ex ** 0.5) * 10
+    del j, ang
+    gpu_ctx.c2c_device(y, y, n, 1, gbfft.INVERSE)  # in place
+    rt = (torch.linalg.vector_norm(y - x) / torch.linalg.vector_norm(x)).item()
+    assert rt < 2e-6
+    del x, y
+    torch.cuda.empty_cache()
+    with pytest.raises(gbfft.GbfftError) as e:
+        gpu_ctx.c2c_device(0, 0, 1 << 31, 1, gbfft.FORWARD)
+    assert e.value.status == gbfft.ERR_UNSUPPORTED

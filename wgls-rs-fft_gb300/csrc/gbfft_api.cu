@@ -50,7 +50,7 @@ struct gbfft_ctx {
     // counter blocks of the fused two-pass form, one per stream so that calls
     // on different streams never share one
     std::map<cudaStream_t, std::unique_ptr<DeviceBuffer>> fused_ctr;
-    uint32_t *d_err = nullptr;  // raised by tensor-core kernels when a bounded wait gives up
+    uint32_t *d_err = nullptr;  // raised by tensor-core and fused kernels when a bounded wait gives up
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
     uint64_t launches = 0;
@@ -149,7 +149,8 @@ int check_device_flag(gbfft_ctx *ctx) {
     GB_CUDA(ctx, cudaMemcpy(&v, ctx->d_err, sizeof v, cudaMemcpyDeviceToHost));
     if (v != 0) {
         GB_CUDA(ctx, cudaMemset(ctx->d_err, 0, sizeof v));
-        return fail(ctx, GBFFT_ERR_TIMEOUT, "a tensor-core completion wait gave up");
+        return fail(ctx, GBFFT_ERR_TIMEOUT,
+                    "a bounded device wait gave up (tensor-core completion or fused-pass dependency)");
     }
     return GBFFT_OK;
 }

@@ -84,6 +84,16 @@ class GpuFft : public FftExecutor {
     }
 
     void set_precision(int precision) { check(gbfft_set_precision(ctx_, precision)); }
+    // Hann window (GBFFT_WINDOW_HANN) or none applied to every loaded sample.
+    void set_window(int window) { check(gbfft_set_window(ctx_, window)); }
+    // The reference pipeline's noise added to every loaded sample (sigma 0: off).
+    void set_noise(uint32_t seed, float sigma) { check(gbfft_set_noise(ctx_, seed, sigma)); }
+    // Times every plan variant for a shape and keeps the fastest; seconds per transform.
+    double autotune(uint64_t n, uint64_t batch, int direction = GBFFT_FORWARD) {
+        double s = 0.0;
+        check(gbfft_autotune(ctx_, n, batch, direction, &s));
+        return s;
+    }
     gbfft_ctx *context() { return ctx_; }
 
    private:
@@ -112,6 +122,30 @@ class GpuFft : public FftExecutor {
     }
 
     gbfft_ctx *ctx_ = nullptr;
+};
+
+// Ragged batch (no reference counterpart): mixed sizes and directions in one
+// persistent launch over device buffers.
+class RaggedPlan {
+   public:
+    RaggedPlan(GpuFft &fft, const std::vector<gbfft_ragged_desc> &descs) : ctx_(fft.context()) {
+        const int st = gbfft_ragged_plan_create(ctx_, descs.data(), (uint32_t)descs.size(), &plan_);
+        if (st != GBFFT_OK) throw Error(st, gbfft_last_error(ctx_));
+    }
+    ~RaggedPlan() { gbfft_ragged_plan_destroy(plan_); }
+    RaggedPlan(const RaggedPlan &) = delete;
+    RaggedPlan &operator=(const RaggedPlan &) = delete;
+    void execute(const void *d_in, void *d_out, uint64_t capacity, bool use_graph = true, void *stream = nullptr) {
+        check(gbfft_ragged_execute(plan_, d_in, d_out, capacity, use_graph ? 1 : 0, stream));
+    }
+    void wait(void *stream = nullptr) { check(gbfft_ragged_wait(plan_, stream)); }
+
+   private:
+    void check(int st) {
+        if (st != GBFFT_OK) throw Error(st, gbfft_last_error(ctx_));
+    }
+    gbfft_ctx *ctx_ = nullptr;
+    gbfft_ragged_plan *plan_ = nullptr;
 };
 
 }  // namespace gbfft

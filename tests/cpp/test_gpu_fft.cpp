@@ -118,6 +118,42 @@ int main() {
         CHECK(std::string(e.what()) == "Transform length must be a non-zero power of two", "%s", e.what());
     }
     CHECK(fft.benchmark_gpu_only(4096, 256, 2, 5) > 0.0, "bench");
+
+    // the window on load equals an explicitly windowed input (tests/test_utils.rs:39-48)
+    {
+        const size_t n = 2048;
+        auto xs = make_input(n);
+        std::vector<Complex> xw(n);
+        for (size_t i = 0; i < n; ++i) {
+            const double w = 0.5 * (1.0 - std::cos(2.0 * M_PI * (double)i / (double)(n - 1)));
+            xw[i] = Complex((float)(xs[i].real() * w), (float)(xs[i].imag() * w));
+        }
+        gbfft::GpuFft wfft;
+        wfft.set_window(GBFFT_WINDOW_HANN);
+        auto a = wfft.fft({xs});
+        auto b = fft.fft({xw});
+        CHECK(max_diff(a[0], b[0]) < 1e-3f, "window on load %g", max_diff(a[0], b[0]));
+        wfft.set_window(GBFFT_WINDOW_NONE);
+        CHECK(max_diff(wfft.fft({xs})[0], fft.fft({xs})[0]) == 0.f, "window off");
+    }
+    // noise on load: zero input gives a non-zero spectrum, the same for the same seed
+    {
+        gbfft::GpuFft nfft;
+        nfft.set_noise(42, 0.1f);
+        auto a = nfft.fft({std::vector<Complex>(1024)});
+        auto b = nfft.fft({std::vector<Complex>(1024)});
+        float mag = 0.f;
+        for (auto &c : a[0]) mag = std::fmax(mag, std::abs(c));
+        CHECK(mag > 0.f && max_diff(a[0], b[0]) == 0.f, "noise on load");
+    }
+    CHECK(fft.autotune(1 << 16, 16) > 0.0, "autotune");
+    try {
+        std::vector<gbfft_ragged_desc> bad{{0, 19, GBFFT_FORWARD}};
+        gbfft::RaggedPlan plan(fft, bad);
+        CHECK(false, "ragged 2^19 not rejected");
+    } catch (const gbfft::Error &e) {
+        CHECK(e.status() == GBFFT_ERR_UNSUPPORTED, "ragged status %d", e.status());
+    }
     CHECK(gbfft_launch_count(fft.context()) > 0, "launches");
 
     std::printf("%s (%d failures)\n", g_fail ? "FAILED" : "OK", g_fail);

@@ -103,12 +103,14 @@ __device__ __forceinline__ void rag_rows(const RagParams &P, const RagItem &it, 
 
 // Returns false when the wait for the first pass gave up.  Eng: the
 // butterfly engine (FP32 registers, or the tensor-core split form).
-template <int LOGR, bool FIRST, class Eng>
+template <int L, bool FIRST, class Eng>
 __device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, float2 *smem, Eng &eng) {
+    // the transform size is a template parameter: strided addresses and
+    // twiddle indices become immediates
+    constexpr int LOGR = FIRST ? rag_logr1(L) : rag_logr2(L);
     constexpr int NG = rag_groups(LOGR);
     __shared__ int s_abort;
     const RagXform x = P.xf[it.a];
-    const int L = x.logn;
     if (!FIRST) {
         if (threadIdx.x == 0) {
             uint32_t polls = 0;
@@ -146,17 +148,18 @@ __device__ __forceinline__ bool rag_pass(const RagParams &P, const RagItem &it, 
     a.keep_l2 = FIRST;
     a.row = 0;
     a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
-    pass_tile<LOGR, NG, FIRST, Eng>(a, smem, eng);
+    pass_tile<LOGR, NG, FIRST, Eng, L, FIRST ? 0 : rag_logr1(L)>(a, smem, eng);
     return true;
 }
 
 template <bool FIRST, class Eng>
 __device__ __forceinline__ bool rag_pass_dispatch(const RagParams &P, const RagItem &it, float2 *smem, Eng &eng) {
-    const int logr = FIRST ? rag_logr1(it.logn) : rag_logr2(it.logn);
-    switch (logr) {
-        case 7: return rag_pass<7, FIRST>(P, it, smem, eng);
-        case 8: return rag_pass<8, FIRST>(P, it, smem, eng);
-        case 9: return rag_pass<9, FIRST>(P, it, smem, eng);
+    switch (it.logn) {
+        case 14: return rag_pass<14, FIRST>(P, it, smem, eng);
+        case 15: return rag_pass<15, FIRST>(P, it, smem, eng);
+        case 16: return rag_pass<16, FIRST>(P, it, smem, eng);
+        case 17: return rag_pass<17, FIRST>(P, it, smem, eng);
+        case 18: return rag_pass<18, FIRST>(P, it, smem, eng);
         default: return true;
     }
 }

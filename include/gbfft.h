@@ -89,7 +89,10 @@ int gbfft_c2c_host(gbfft_ctx *ctx, const float *in, float *out, uint64_t n,
  * (src/lib.rs:433, 517-533): `batch` separate rows, row i at in_rows[i] with
  * row_lengths[i] complex values, result row i written to out_rows[i].
  * All lengths must be equal (GBFFT_ERR_LENGTH_MISMATCH) and a power of two
- * (GBFFT_ERR_INVALID_SIZE), checked in the reference's order. */
+ * (GBFFT_ERR_INVALID_SIZE), checked in the reference's order.  Rows are
+ * copied to and from pinned staging chunk by chunk while earlier chunks are
+ * on the device, so out_rows[i] may be in_rows[i] (in place) but must not
+ * overlap any other input row. */
 int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows,
                         const uint64_t *row_lengths, float *const *out_rows,
                         uint64_t batch, int direction);

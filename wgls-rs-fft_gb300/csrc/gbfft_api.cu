@@ -10,10 +10,12 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -328,6 +330,92 @@ int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64
     return run_variant(ctx, in, out, n, batch, direction, v, stream, row_base);
 }
 
+// Copy rows [r0, r1) between caller memory and the pinned stage (rows back to
+// back), split by stage byte ranges over up to kCopyThreads host threads (one
+// thread below 8 MB), so even a single large row is copied in parallel.
+constexpr unsigned kCopyThreads = 8;
+template <class RowPtr>
+static void copy_rows(char *stage, RowPtr row, uint64_t r0, uint64_t r1, size_t row_bytes, bool to_stage) {
+    auto work = [&](size_t a, size_t b) {
+        while (a < b) {
+            const uint64_t r = a / row_bytes;
+            const size_t off = a - r * row_bytes;
+            const size_t len = std::min(b - a, row_bytes - off);
+            char *caller = (char *)row(r) + off;
+            if (to_stage) memcpy(stage + a, caller, len);
+            else memcpy(caller, stage + a, len);
+            a += len;
+        }
+    };
+    const size_t a0 = (size_t)r0 * row_bytes, a1 = (size_t)r1 * row_bytes;
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const unsigned nt = std::min(kCopyThreads, hw);
+    if (a1 - a0 < ((size_t)8 << 20) || nt < 2) {
+        work(a0, a1);
+        return;
+    }
+    const size_t piece = (((a1 - a0) / nt) + 4095) & ~(size_t)4095;
+    std::vector<std::thread> th;
+    for (unsigned k = 1; k < nt && a0 + k * piece < a1; ++k)
+        th.emplace_back(work, a0 + k * piece, std::min(a1, a0 + (k + 1) * piece));
+    work(a0, std::min(a1, a0 + piece));
+    for (auto &t : th) t.join();
+}
+
+// Host batch: split into chunks of whole transforms and pipeline
+// H2D -> transform -> D2H over three streams, so the two copy directions and
+// the kernels overlap.  Pinned contiguous buffers are used as they are;
+// otherwise (pageable buffers or separate rows, row(r) giving transform r's
+// host address) each chunk is copied into pinned staging just before its
+// H2D, and out of it once its D2H is done -- two chunks later, while the
+// device works on the chunks in between.
+template <class InRow, class OutRow>
+static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, const float *pin_in,
+                         float *pin_out, InRow in_row, OutRow out_row) {
+    const size_t row_bytes = (size_t)n * sizeof(float2);
+    const size_t bytes = row_bytes * batch;
+    int st = ctx->dbuf.ensure(bytes, ctx->err);
+    if (st != GBFFT_OK) return st;
+    float2 *d = (float2 *)ctx->dbuf.ptr;
+    const bool staged = !(pin_in && pin_out);
+    if (staged) {
+        st = ensure_hstage(ctx, bytes);
+        if (st != GBFFT_OK) return st;
+    }
+    char *stage = (char *)ctx->hstage;
+    const char *src = staged ? stage : (const char *)pin_in;
+    char *dst = staged ? stage : (char *)pin_out;
+    uint64_t rows_per_chunk = row_bytes >= ctx->host_chunk ? 1 : ctx->host_chunk / row_bytes;
+    if (log2u(n) > kRowsMaxLogN) rows_per_chunk = batch;  // multi-pass shares one workspace: no overlap
+    std::vector<std::pair<uint64_t, uint64_t>> chunks;
+    for (uint64_t r = 0; r < batch; r += rows_per_chunk) chunks.emplace_back(r, std::min(batch, r + rows_per_chunk));
+    auto drain = [&](size_t c) -> int {  // chunk c's D2H is done: copy it out
+        GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[c % 3]));
+        if (staged) copy_rows(stage, out_row, chunks[c].first, chunks[c].second, row_bytes, false);
+        return GBFFT_OK;
+    };
+    for (size_t c = 0; c < chunks.size(); ++c) {
+        const uint64_t r0 = chunks[c].first, rows = chunks[c].second - chunks[c].first;
+        const size_t off = (size_t)r0 * row_bytes, len = (size_t)rows * row_bytes;
+        if (c >= 3) {  // chunk c reuses the stream of chunk c - 3
+            st = drain(c - 3);
+            if (st != GBFFT_OK) return st;
+        }
+        if (staged) copy_rows(stage, in_row, r0, r0 + rows, row_bytes, true);
+        cudaStream_t s = ctx->xfer[c % 3];
+        GB_CUDA(ctx, cudaMemcpyAsync((char *)d + off, src + off, len, cudaMemcpyHostToDevice, s));
+        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)d + off), n, rows, direction, s,
+                        r0);
+        if (st != GBFFT_OK) return st;
+        GB_CUDA(ctx, cudaMemcpyAsync(dst + off, (char *)d + off, len, cudaMemcpyDeviceToHost, s));
+    }
+    for (size_t c = chunks.size() >= 3 ? chunks.size() - 3 : 0; c < chunks.size(); ++c) {
+        st = drain(c);
+        if (st != GBFFT_OK) return st;
+    }
+    return check_device_flag(ctx);
+}
+
 }  // namespace
 
 extern "C" {
@@ -463,47 +551,11 @@ int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n, 
 // Host batch already contiguous in `in` (pinned or pageable).
 static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t n, uint64_t batch,
                            int direction) {
-    const size_t bytes = (size_t)n * batch * sizeof(float2);
-    int st = ctx->dbuf.ensure(bytes, ctx->err);
-    if (st != GBFFT_OK) return st;
-    float2 *d = (float2 *)ctx->dbuf.ptr;
-    const bool pinned = host_is_pinned(in) && host_is_pinned(out);
-    const float *src = in;
-    float *dst = out;
-    if (!pinned) {
-        st = ensure_hstage(ctx, bytes);
-        if (st != GBFFT_OK) return st;
-        memcpy(ctx->hstage, in, bytes);
-        src = (const float *)ctx->hstage;
-        dst = (float *)ctx->hstage;
-    }
-    // Split the batch into chunks of whole transforms and pipeline
-    // H2D -> transform -> D2H over three streams so the two copy directions and
-    // the kernels overlap.
     const size_t row_bytes = (size_t)n * sizeof(float2);
-    const size_t chunk_target = ctx->host_chunk;
-    uint64_t rows_per_chunk = row_bytes >= chunk_target ? 1 : chunk_target / row_bytes;
-    if (log2u(n) > kRowsMaxLogN) rows_per_chunk = batch;  // multi-pass shares one workspace: no overlap
-    uint64_t done = 0;
-    int k = 0;
-    while (done < batch) {
-        const uint64_t rows = (batch - done) < rows_per_chunk ? (batch - done) : rows_per_chunk;
-        const size_t off = (size_t)done * row_bytes;
-        const size_t len = (size_t)rows * row_bytes;
-        cudaStream_t s = ctx->xfer[k % 3];
-        GB_CUDA(ctx, cudaMemcpyAsync((char *)d + off, (const char *)src + off, len, cudaMemcpyHostToDevice, s));
-        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)d + off), n, rows, direction, s,
-                        done);
-        if (st != GBFFT_OK) return st;
-        GB_CUDA(ctx, cudaMemcpyAsync((char *)dst + off, (char *)d + off, len, cudaMemcpyDeviceToHost, s));
-        done += rows;
-        ++k;
-    }
-    for (auto s : ctx->xfer) GB_CUDA(ctx, cudaStreamSynchronize(s));
-    st = check_device_flag(ctx);
-    if (st != GBFFT_OK) return st;
-    if (!pinned) memcpy(out, ctx->hstage, bytes);
-    return GBFFT_OK;
+    const bool pinned = host_is_pinned(in) && host_is_pinned(out);
+    auto in_row = [&](uint64_t r) { return (const char *)in + r * row_bytes; };
+    auto out_row = [&](uint64_t r) { return (char *)out + r * row_bytes; };
+    return host_pipeline(ctx, n, batch, direction, pinned ? in : nullptr, pinned ? out : nullptr, in_row, out_row);
 }
 
 int gbfft_c2c_host(gbfft_ctx *ctx, const float *in, float *out, uint64_t n, uint64_t batch, int direction) {
@@ -533,16 +585,9 @@ int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows, const uint6
     for (uint64_t i = 0; i < batch; ++i)
         if (!in_rows[i] || !out_rows[i]) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null row pointer");
     GB_CUDA(ctx, cudaSetDevice(ctx->device));
-    const size_t row_bytes = (size_t)n * sizeof(float2);
-    const size_t bytes = row_bytes * batch;
-    st = ensure_hstage(ctx, bytes);
-    if (st != GBFFT_OK) return st;
-    char *stage = (char *)ctx->hstage;
-    for (uint64_t i = 0; i < batch; ++i) memcpy(stage + i * row_bytes, in_rows[i], row_bytes);
-    st = host_contiguous(ctx, (const float *)stage, (float *)stage, n, batch, direction);
-    if (st != GBFFT_OK) return st;
-    for (uint64_t i = 0; i < batch; ++i) memcpy(out_rows[i], stage + i * row_bytes, row_bytes);
-    return GBFFT_OK;
+    auto in_row = [&](uint64_t r) { return (const char *)in_rows[r]; };
+    auto out_row = [&](uint64_t r) { return (char *)out_rows[r]; };
+    return host_pipeline(ctx, n, batch, direction, nullptr, nullptr, in_row, out_row);
 }
 
 int gbfft_ragged_plan_create(gbfft_ctx *ctx, const gbfft_ragged_desc *descs, uint32_t count,

@@ -48,6 +48,7 @@ struct gbfft_ctx {
     std::string tune_cache;
     DeviceBuffer tune_a, tune_b;  // scratch for the autotuner
     DeviceBuffer dbuf;    // device copy of a host batch
+    DeviceBuffer dbuf_out;  // its transform (out of place: fused pairs, no shared workspace)
     DeviceBuffer ws;      // multi-pass workspace
     // counter blocks of the fused two-pass form, one per stream so that calls
     // on different streams never share one
@@ -375,8 +376,10 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
     const size_t row_bytes = (size_t)n * sizeof(float2);
     const size_t bytes = row_bytes * batch;
     int st = ctx->dbuf.ensure(bytes, ctx->err);
+    if (st == GBFFT_OK) st = ctx->dbuf_out.ensure(bytes, ctx->err);
     if (st != GBFFT_OK) return st;
     float2 *d = (float2 *)ctx->dbuf.ptr;
+    float2 *dy = (float2 *)ctx->dbuf_out.ptr;
     const bool staged = !(pin_in && pin_out);
     if (staged) {
         st = ensure_hstage(ctx, bytes);
@@ -386,7 +389,14 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
     const char *src = staged ? stage : (const char *)pin_in;
     char *dst = staged ? stage : (char *)pin_out;
     uint64_t rows_per_chunk = row_bytes >= ctx->host_chunk ? 1 : ctx->host_chunk / row_bytes;
-    if (log2u(n) > kRowsMaxLogN) rows_per_chunk = batch;  // multi-pass shares one workspace: no overlap
+    if (log2u(n) > kRowsMaxLogN && rows_per_chunk < batch) {
+        // plans of three or more passes share the context's workspace: one chunk
+        const PlanVariant v = choose_variant(ctx, log2u(n), rows_per_chunk, direction, st);
+        Plan *plan = nullptr;
+        if (st == GBFFT_OK) st = get_plan(ctx, log2u(n), v, &plan);
+        if (st != GBFFT_OK) return st;
+        if (plan->passes.size() >= 3) rows_per_chunk = batch;
+    }
     std::vector<std::pair<uint64_t, uint64_t>> chunks;
     for (uint64_t r = 0; r < batch; r += rows_per_chunk) chunks.emplace_back(r, std::min(batch, r + rows_per_chunk));
     auto drain = [&](size_t c) -> int {  // chunk c's D2H is done: copy it out
@@ -404,10 +414,10 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
         if (staged) copy_rows(stage, in_row, r0, r0 + rows, row_bytes, true);
         cudaStream_t s = ctx->xfer[c % 3];
         GB_CUDA(ctx, cudaMemcpyAsync((char *)d + off, src + off, len, cudaMemcpyHostToDevice, s));
-        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)d + off), n, rows, direction, s,
+        st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)dy + off), n, rows, direction, s,
                         r0);
         if (st != GBFFT_OK) return st;
-        GB_CUDA(ctx, cudaMemcpyAsync(dst + off, (char *)d + off, len, cudaMemcpyDeviceToHost, s));
+        GB_CUDA(ctx, cudaMemcpyAsync(dst + off, (char *)dy + off, len, cudaMemcpyDeviceToHost, s));
     }
     for (size_t c = chunks.size() >= 3 ? chunks.size() - 3 : 0; c < chunks.size(); ++c) {
         st = drain(c);
@@ -492,6 +502,7 @@ void gbfft_destroy(gbfft_ctx *ctx) {
         }
     ctx->plans.clear();
     ctx->dbuf.release();
+    ctx->dbuf_out.release();
     ctx->ws.release();
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->hstage) cudaFreeHost(ctx->hstage);

@@ -11,8 +11,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <algorithm>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <thread>
@@ -28,6 +31,64 @@ using namespace gbfft;
 struct gbfft_ragged_plan {
     gbfft_ctx *ctx;
     RaggedPlanImpl *impl;
+};
+
+// Host threads that copy a batch between caller memory and pinned staging:
+// started on first use, kept for the context's life.  run(f) calls f(k, n)
+// on the calling thread (k = 0) and every worker (k = 1 .. n-1) and returns
+// when all have finished.
+class CopyPool {
+   public:
+    explicit CopyPool(unsigned n) : n_(n) {
+        for (unsigned k = 1; k < n_; ++k) workers_.emplace_back([this, k] { loop(k); });
+    }
+    ~CopyPool() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (auto &t : workers_) t.join();
+    }
+    unsigned size() const { return n_; }
+    void run(const std::function<void(unsigned, unsigned)> &f) {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            job_ = &f;
+            pending_ = n_ - 1;
+            ++gen_;
+        }
+        cv_.notify_all();
+        f(0, n_);
+        std::unique_lock<std::mutex> l(m_);
+        done_.wait(l, [this] { return pending_ == 0; });
+        job_ = nullptr;
+    }
+
+   private:
+    void loop(unsigned k) {
+        unsigned seen = 0;
+        for (;;) {
+            const std::function<void(unsigned, unsigned)> *job;
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return stop_ || gen_ != seen; });
+                if (stop_) return;
+                seen = gen_;
+                job = job_;
+            }
+            (*job)(k, n_);
+            std::lock_guard<std::mutex> g(m_);
+            if (--pending_ == 0) done_.notify_one();
+        }
+    }
+    unsigned n_;
+    std::vector<std::thread> workers_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    const std::function<void(unsigned, unsigned)> *job_ = nullptr;
+    unsigned pending_ = 0, gen_ = 0;
+    bool stop_ = false;
 };
 
 struct gbfft_ctx {
@@ -49,6 +110,7 @@ struct gbfft_ctx {
     DeviceBuffer tune_a, tune_b;  // scratch for the autotuner
     DeviceBuffer dbuf;    // device copy of a host batch
     DeviceBuffer dbuf_out;  // its transform (out of place: fused pairs, no shared workspace)
+    std::unique_ptr<CopyPool> copy_pool;  // staging copies of pageable host batches
     DeviceBuffer ws;      // multi-pass workspace
     // counter blocks of the fused two-pass form, one per stream so that calls
     // on different streams never share one
@@ -332,11 +394,12 @@ int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64
 }
 
 // Copy rows [r0, r1) between caller memory and the pinned stage (rows back to
-// back), split by stage byte ranges over up to kCopyThreads host threads (one
+// back), split by stage byte ranges over the context's copy threads (one
 // thread below 8 MB), so even a single large row is copied in parallel.
 constexpr unsigned kCopyThreads = 8;
 template <class RowPtr>
-static void copy_rows(char *stage, RowPtr row, uint64_t r0, uint64_t r1, size_t row_bytes, bool to_stage) {
+static void copy_rows(gbfft_ctx *ctx, char *stage, RowPtr row, uint64_t r0, uint64_t r1, size_t row_bytes,
+                      bool to_stage) {
     auto work = [&](size_t a, size_t b) {
         while (a < b) {
             const uint64_t r = a / row_bytes;
@@ -349,18 +412,20 @@ static void copy_rows(char *stage, RowPtr row, uint64_t r0, uint64_t r1, size_t 
         }
     };
     const size_t a0 = (size_t)r0 * row_bytes, a1 = (size_t)r1 * row_bytes;
-    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-    const unsigned nt = std::min(kCopyThreads, hw);
-    if (a1 - a0 < ((size_t)8 << 20) || nt < 2) {
+    if (a1 - a0 < ((size_t)8 << 20)) {
         work(a0, a1);
         return;
     }
+    if (!ctx->copy_pool) {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        ctx->copy_pool.reset(new CopyPool(std::min(kCopyThreads, hw)));
+    }
+    const unsigned nt = ctx->copy_pool->size();
     const size_t piece = (((a1 - a0) / nt) + 4095) & ~(size_t)4095;
-    std::vector<std::thread> th;
-    for (unsigned k = 1; k < nt && a0 + k * piece < a1; ++k)
-        th.emplace_back(work, a0 + k * piece, std::min(a1, a0 + (k + 1) * piece));
-    work(a0, std::min(a1, a0 + piece));
-    for (auto &t : th) t.join();
+    ctx->copy_pool->run([&](unsigned k, unsigned) {
+        const size_t a = a0 + k * piece;
+        if (a < a1) work(a, std::min(a1, a + piece));
+    });
 }
 
 // Host batch: split into chunks of whole transforms and pipeline
@@ -401,7 +466,7 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
     for (uint64_t r = 0; r < batch; r += rows_per_chunk) chunks.emplace_back(r, std::min(batch, r + rows_per_chunk));
     auto drain = [&](size_t c) -> int {  // chunk c's D2H is done: copy it out
         GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[c % 3]));
-        if (staged) copy_rows(stage, out_row, chunks[c].first, chunks[c].second, row_bytes, false);
+        if (staged) copy_rows(ctx, stage, out_row, chunks[c].first, chunks[c].second, row_bytes, false);
         return GBFFT_OK;
     };
     for (size_t c = 0; c < chunks.size(); ++c) {
@@ -411,7 +476,7 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
             st = drain(c - 3);
             if (st != GBFFT_OK) return st;
         }
-        if (staged) copy_rows(stage, in_row, r0, r0 + rows, row_bytes, true);
+        if (staged) copy_rows(ctx, stage, in_row, r0, r0 + rows, row_bytes, true);
         cudaStream_t s = ctx->xfer[c % 3];
         GB_CUDA(ctx, cudaMemcpyAsync((char *)d + off, src + off, len, cudaMemcpyHostToDevice, s));
         st = run_device(ctx, (const float2 *)((char *)d + off), (float2 *)((char *)dy + off), n, rows, direction, s,

@@ -395,7 +395,7 @@ int run_device(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint64
 
 // Copy rows [r0, r1) between caller memory and the pinned stage (rows back to
 // back), split by stage byte ranges over the context's copy threads (one
-// thread below 8 MB), so even a single large row is copied in parallel.
+// thread below 1 MB), so even a single large row is copied in parallel.
 constexpr unsigned kCopyThreads = 8;
 template <class RowPtr>
 static void copy_rows(gbfft_ctx *ctx, char *stage, RowPtr row, uint64_t r0, uint64_t r1, size_t row_bytes,
@@ -412,7 +412,7 @@ static void copy_rows(gbfft_ctx *ctx, char *stage, RowPtr row, uint64_t r0, uint
         }
     };
     const size_t a0 = (size_t)r0 * row_bytes, a1 = (size_t)r1 * row_bytes;
-    if (a1 - a0 < ((size_t)8 << 20)) {
+    if (a1 - a0 < ((size_t)1 << 20)) {
         work(a0, a1);
         return;
     }

@@ -351,3 +351,24 @@ def test_host_pageable_batch_many_chunks(gpu_ctx, oracle):
         assert oracle.rel_l2(y[i], oracle.fft64(x[i:i + 1])[0]) <= TOL_REL_L2
     z = gpu_ctx.c2c_host(y, gbfft.INVERSE)
     assert oracle.rel_l2(z, x) <= 1e-6
+
+
+@pytest.mark.parametrize("logn,batch", [(10, 33), (12, 5), (14, 3), (16, 5), (18, 2), (22, 1)])
+def test_device_entry_eight_byte_aligned_pointers(gpu_ctx, oracle, torch_cuda, logn, batch):
+    """Input and output one sample into their allocations (8-byte, not 16-byte,
+    aligned): single pass, fused pairs and the three-pass form."""
+    import gbfft
+    from gbfft import signals
+    torch = torch_cuda
+    n = 1 << logn
+    x = signals.uniform_c64(batch, n, seed=720 + logn)
+    big_in = torch.zeros(batch * n + 1, dtype=torch.complex64, device="cuda")
+    big_out = torch.full((batch * n + 2,), float("nan"), dtype=torch.complex64, device="cuda")
+    big_in[1:].copy_(torch.from_numpy(x.reshape(-1)))
+    d_in, d_out = big_in[1:], big_out[1:batch * n + 1]
+    assert d_in.data_ptr() % 16 == 8 and d_out.data_ptr() % 16 == 8
+    gpu_ctx.c2c_device(d_in, d_out, n, batch, gbfft.FORWARD)
+    torch.cuda.synchronize()
+    y = d_out.cpu().numpy().reshape(batch, n)
+    assert oracle.rel_l2(y, oracle.fft64(x)) <= TOL_REL_L2
+    assert torch.isnan(big_out[0]).item() and torch.isnan(big_out[-1]).item()  # neighbours untouched

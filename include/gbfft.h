@@ -208,7 +208,8 @@ int gbfft_set_noise(gbfft_ctx *ctx, uint32_t seed, float sigma);
 /* Autotuner (no reference counterpart; the reference's find_optimal_batch
  * example only sweeps batch sizes, examples/find_optimal_batch.rs:28).  Times
  * every plan variant for (n, batch, direction, current precision) -- global
- * pass split and plain vs persistent tile-loop kernels -- on the context's own
+ * pass split, plain or persistent tile-loop kernels, fused pass pairs, and
+ * transforms per CTA of the single-pass kernel -- on the context's own
  * scratch buffers (caller data is never touched), keeps the fastest for later
  * calls with that size, direction, precision and a batch of the same power of
  * two, and writes the mean seconds per transform of the winner.  If the
@@ -217,6 +218,14 @@ int gbfft_set_noise(gbfft_ctx *ctx, uint32_t seed, float sigma);
  * GBFFT_AUTOTUNE=1 makes the first call of every untuned combination tune
  * itself. */
 int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *best_seconds);
+
+/* Environment read by the library:
+ *   GBFFT_AUTOTUNE, GBFFT_AUTOTUNE_CACHE   see gbfft_autotune
+ *   GBFFT_PRECISION=tc_fp16|tc_bf16x3      default precision of new contexts
+ *   GBFFT_HOST_CHUNK_BYTES=<bytes>         chunk of the host-batch pipeline (32 MB)
+ *   GBFFT_DEVICE_ALLOC_CAP=<bytes>         device requests above it fail with
+ *                                          GBFFT_ERR_OUT_OF_MEMORY (tests the
+ *                                          out-of-memory paths without a real one) */
 
 /* Number of kernel launches this context has issued since creation (all
  * entry points).  Lets callers count GPU work without a profiler. */

@@ -372,3 +372,56 @@ def test_device_entry_eight_byte_aligned_pointers(gpu_ctx, oracle, torch_cuda, l
     y = d_out.cpu().numpy().reshape(batch, n)
     assert oracle.rel_l2(y, oracle.fft64(x)) <= TOL_REL_L2
     assert torch.isnan(big_out[0]).item() and torch.isnan(big_out[-1]).item()  # neighbours untouched
+
+
+# ---- exhaustive small sizes, configuration from the environment, out of memory ---------
+
+@pytest.mark.parametrize("logn", range(0, 7))
+def test_small_sizes_every_batch(gpu_ctx, oracle, logn):
+    """N = 1 .. 64, every batch size 1 .. 5, both directions, against the
+    reference path (1e-3) and FP64 (2e-6)."""
+    import gbfft
+    from gbfft import signals
+    n = 1 << logn
+    for batch in range(1, 6):
+        x = signals.normal_c64(batch, n, seed=900 + 10 * logn + batch)
+        for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+            y = gpu_ctx.c2c_host(x, d)
+            assert oracle.max_abs_err(y, oracle.ref_fft(x, inverse=inv)) <= TOL_REF, (n, batch, inv)
+            assert oracle.rel_l2(y, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2, (n, batch, inv)
+
+
+def test_precision_from_environment(lib_built, monkeypatch):
+    import gbfft
+    monkeypatch.setenv("GBFFT_PRECISION", "tc_fp16")
+    with gbfft.Context(0) as ctx:  # the split form covers N >= 2^15 only
+        with pytest.raises(gbfft.GbfftError) as e:
+            ctx.c2c_host(np.ones((1, 256), np.complex64), gbfft.FORWARD)
+        assert e.value.status == gbfft.ERR_UNSUPPORTED
+    monkeypatch.delenv("GBFFT_PRECISION")
+    with gbfft.Context(0) as ctx:
+        assert np.allclose(ctx.c2c_host(np.ones((1, 256), np.complex64), gbfft.FORWARD)[0][0], 256)
+
+
+def test_out_of_memory_paths(lib_built, monkeypatch, oracle, torch_cuda):
+    """GBFFT_DEVICE_ALLOC_CAP makes device allocations above it fail: every
+    entry reports GBFFT_ERR_OUT_OF_MEMORY with its message, leaves caller data
+    alone, and the same context works once the cap is lifted."""
+    import gbfft
+    from gbfft import signals
+    torch = torch_cuda
+    x = signals.normal_c64(8, 1 << 16, seed=910)  # 4 MB
+    monkeypatch.setenv("GBFFT_DEVICE_ALLOC_CAP", str(1 << 20))
+    with gbfft.Context(0) as ctx:
+        with pytest.raises(gbfft.GbfftError) as e:  # host batch: device copy of the batch
+            ctx.c2c_host(x, gbfft.FORWARD)
+        assert e.value.status == gbfft.ERR_OUT_OF_MEMORY and "GBFFT_DEVICE_ALLOC_CAP" in str(e.value)
+        d = torch.from_numpy(x).cuda()
+        with pytest.raises(gbfft.GbfftError) as e:  # in place two-pass: workspace
+            ctx.c2c_device(d, d, 1 << 16, 8, gbfft.FORWARD)
+        assert e.value.status == gbfft.ERR_OUT_OF_MEMORY
+        torch.cuda.synchronize()
+        assert np.array_equal(d.cpu().numpy(), x)
+        monkeypatch.delenv("GBFFT_DEVICE_ALLOC_CAP")
+        y = ctx.c2c_host(x, gbfft.FORWARD)
+        assert oracle.rel_l2(y, oracle.fft64(x)) <= TOL_REL_L2

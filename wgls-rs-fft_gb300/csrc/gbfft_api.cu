@@ -542,6 +542,10 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
         return GBFFT_ERR_CUDA;
     if (cudaMalloc(&ctx->d_err, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_OUT_OF_MEMORY;
     if (cudaMemset(ctx->d_err, 0, sizeof(uint32_t)) != cudaSuccess) return GBFFT_ERR_CUDA;
+    if (const char *c = getenv("GBFFT_PRECISION")) {  // default precision of new contexts
+        if (!strcmp(c, "tc_fp16")) ctx->precision = GBFFT_PREC_TC_FP16;
+        else if (!strcmp(c, "tc_bf16x3")) ctx->precision = GBFFT_PREC_TC_BF16X3;
+    }
     if (const char *c = getenv("GBFFT_HOST_CHUNK_BYTES")) {
         const long long v = atoll(c);
         if (v >= (1 << 16)) ctx->host_chunk = (size_t)v;

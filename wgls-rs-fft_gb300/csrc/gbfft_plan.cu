@@ -1,13 +1,25 @@
 // Plan construction and execution (see gbfft_plan.h).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "gbfft_plan.h"
 
 namespace gbfft {
 
+// GBFFT_DEVICE_ALLOC_CAP=<bytes>: requests above it fail as if the device were
+// out of memory (exercises the out-of-memory paths without exhausting a GPU).
+static bool over_alloc_cap(size_t want) {
+    const char *c = getenv("GBFFT_DEVICE_ALLOC_CAP");
+    return c && *c && want > (size_t)strtoull(c, nullptr, 10);
+}
+
 int DeviceBuffer::ensure(size_t want, std::string &err) {
     if (bytes >= want) return GBFFT_OK;
+    if (over_alloc_cap(want)) {
+        err = std::string("device allocation of ") + std::to_string(want) + " bytes exceeds GBFFT_DEVICE_ALLOC_CAP";
+        return GBFFT_ERR_OUT_OF_MEMORY;
+    }
     release();
     cudaError_t e = cudaMalloc(&ptr, want);
     if (e != cudaSuccess) {

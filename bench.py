@@ -271,7 +271,8 @@ def run_ragged(args, ctx, dev, rank, world):
     descs, total = signals.ragged_set(args.ragged_count, seed=5)
     x = signals.uniform_c64_torch(1, total, seed=5, device=dev)[0]
     y = torch.empty_like(x)
-    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3}[args.precision]
+    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3,
+            "tc_tf32": gbfft.PREC_TC_TF32}[args.precision]
     ctx.set_precision(prec)  # the plan takes the context's precision
     plan = ctx.ragged_plan(descs)
     # the uniform comparison: the split form where the uniform entry has it (N >= 2^15)
@@ -385,7 +386,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ragged_c5"], default=DEFAULT_WORKLOAD)
-    ap.add_argument("--precision", choices=["fp32", "tc_fp16", "tc_bf16x3"], default="fp32")
+    ap.add_argument("--precision", choices=["fp32", "tc_fp16", "tc_bf16x3", "tc_tf32"], default="fp32")
     ap.add_argument("--window", choices=["none", "hann"], default="none",
                     help="Hann window fused into every transform's load")
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -421,7 +422,8 @@ def main():
     logn, batch, distn, seed = WORKLOADS[workload]
     n = 1 << logn
     x = make_input(logn, batch, distn, seed, dev, ctx)
-    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3}[args.precision]
+    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3,
+            "tc_tf32": gbfft.PREC_TC_TF32}[args.precision]
     ctx.set_precision(prec)
     ctx.set_window(gbfft.WINDOW_HANN if args.window == "hann" else gbfft.WINDOW_NONE)
     y = torch.empty_like(x)

@@ -53,7 +53,10 @@ typedef enum gbfft_precision {
     GBFFT_PREC_TC_FP16 = 1,   /* radix-16 sub-DFTs as tcgen05 matrix products, FP16 hi+lo operands
                                  (3 products), per-vector power-of-two scaling, FP32 accumulation;
                                  multi-pass sizes N >= 2^15 */
-    GBFFT_PREC_TC_BF16X3 = 2  /* same with BF16 hi+lo operands */
+    GBFFT_PREC_TC_BF16X3 = 2, /* same with BF16 hi+lo operands */
+    GBFFT_PREC_TC_TF32 = 3    /* same with TF32 hi+lo operands (hi = the value rounded to TF32,
+                                 lo = the exact rest); TF32 keeps FP32's exponent range, so no
+                                 scaling */
 } gbfft_precision;
 
 typedef struct gbfft_ctx gbfft_ctx;
@@ -221,7 +224,7 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
 
 /* Environment read by the library:
  *   GBFFT_AUTOTUNE, GBFFT_AUTOTUNE_CACHE   see gbfft_autotune
- *   GBFFT_PRECISION=tc_fp16|tc_bf16x3      default precision of new contexts
+ *   GBFFT_PRECISION=tc_fp16|tc_bf16x3|tc_tf32  default precision of new contexts
  *   GBFFT_HOST_CHUNK_BYTES=<bytes>         chunk of the host-batch pipeline (32 MB)
  *   GBFFT_DEVICE_ALLOC_CAP=<bytes>         device requests above it fail with
  *                                          GBFFT_ERR_OUT_OF_MEMORY (tests the

@@ -73,6 +73,7 @@ struct FusedParams {
     uint32_t *ctr;      // [0] next item, [1] CTAs finished, [2 + group] A tiles published
     uint32_t *err;
     uint32_t spin_limit;
+    const uint4 *gtab;  // split forms: the G operand table (fft_passes_tc.cu)
 };
 
 __device__ __forceinline__ uint32_t fused_ld_acquire(const uint32_t *p) {
@@ -113,12 +114,14 @@ __device__ __forceinline__ uint32_t fused_claim(const FusedParams &P) {
     return *(volatile uint32_t *)P.err != 0u ? 0xffffffffu : atomicAdd(P.ctr, 1u);
 }
 
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA>
-__global__ void __launch_bounds__(THREADS, (FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA>::MINB))
-fft_fused_kernel(FusedParams P) {
+// The queue loop of one CTA: claims items until the queue (or the launch,
+// after an error) is exhausted.  `Eng` runs the radix-16 butterflies (FP32
+// registers, or the tensor cores for the split forms); every thread of the
+// CTA takes part in every item.
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, class Eng>
+__device__ __forceinline__ void fused_loop(const FusedParams &P, float2 *smem_f, Eng eng) {
     using C = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA>;
     constexpr uint32_t T = C::T, GPT = C::GPT;
-    extern __shared__ float2 smem_f[];
     // Claimed queue positions, double-buffered: slot `par` holds the current
     // item, slot par ^ 1 receives the next claim while the tile runs.
     __shared__ uint32_t s_item[2];
@@ -157,7 +160,7 @@ fft_fused_kernel(FusedParams P) {
             a.coherent_load = false;
             a.keep_l2 = true;
             a.ops = C::FIRST_A ? P.ops : LoadOps{nullptr, 0u, 0.f, 0u};
-            pass_tile<LOGRA, C::NGA, C::FIRST_A, DftRegs, LOGN, LOGPA>(a, smem_f);
+            pass_tile<LOGRA, C::NGA, C::FIRST_A, Eng, LOGN, LOGPA>(a, smem_f, eng);
         } else {
             if (threadIdx.x == 0) {
                 uint32_t polls = 0;
@@ -184,7 +187,7 @@ fft_fused_kernel(FusedParams P) {
             a.out_im = P.out_im;
             a.coherent_load = true;
             a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
-            pass_tile<LOGRB, C::NGB, false, DftRegs, LOGN, C::LOGPB>(a, smem_f);
+            pass_tile<LOGRB, C::NGB, false, Eng, LOGN, C::LOGPB>(a, smem_f, eng);
         }
         __syncthreads();  // the tile's stores are issued; shared memory is free
         if (threadIdx.x == 0) {
@@ -196,8 +199,12 @@ fft_fused_kernel(FusedParams P) {
             }
         }
     }
-    // The last CTA to finish clears the counters for the next launch; every
-    // other CTA has published all its work before it counts itself out.
+}
+
+// The last CTA to finish clears the counters for the next launch; every
+// other CTA has published all its work before it counts itself out.
+template <int THREADS>
+__device__ __forceinline__ void fused_finish(const FusedParams &P) {
     __shared__ int s_last;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -209,6 +216,14 @@ fft_fused_kernel(FusedParams P) {
         __threadfence();
         for (uint32_t i = threadIdx.x; i < 2u + P.ngroups; i += THREADS) P.ctr[i] = 0u;
     }
+}
+
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA>
+__global__ void __launch_bounds__(THREADS, (FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA>::MINB))
+fft_fused_kernel(FusedParams P) {
+    extern __shared__ float2 smem_f[];
+    fused_loop<LOGRA, LOGRB, THREADS, LOGN, LOGPA>(P, smem_f, DftRegs());
+    fused_finish<THREADS>(P);
 }
 
 template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA>

@@ -30,7 +30,28 @@ cudaError_t fused_prepare(FusedDesc &d) {
         e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem);
         if (e != cudaSuccess) return e;
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctas_per_sm, d.fn, d.threads, d.smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.ctas_per_sm, d.fn, d.threads, d.smem);
+    if (e != cudaSuccess || d.tmem_cols <= 0) return e;
+    // Split forms: the occupancy query answers 1 for kernels that allocate
+    // tensor memory, although the SM runs as many such CTAs as registers and
+    // shared memory allow (tcgen05.alloc only waits while the SM's 512 TMEM
+    // columns are taken, and each CTA allocates before it claims any work, so
+    // such a wait never holds up a dependency).  Count them from the kernel's
+    // resources, bounded by the columns each CTA holds for its whole run.
+    cudaFuncAttributes fa;
+    int dev = 0, smem_sm = 0, regs_sm = 0, threads_sm = 0;
+    if ((e = cudaFuncGetAttributes(&fa, d.fn)) != cudaSuccess) return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev)) != cudaSuccess) return e;
+    const int warps = (d.threads + 31) / 32;
+    const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * 32 * warps;  // allocated per warp in units of 8 per thread
+    const size_t smem_cta = d.smem + fa.sharedSizeBytes + 1024;      // 1 KB reserved per CTA
+    int fit = std::min(regs_sm / std::max(1, regs_cta), threads_sm / std::max(1, d.threads));
+    fit = std::min<int>(fit, (int)(smem_sm / smem_cta));
+    d.ctas_per_sm = std::max(1, std::min(std::max(d.ctas_per_sm, fit), 512 / d.tmem_cols));
+    return cudaSuccess;
 }
 
 uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms) {
@@ -46,7 +67,8 @@ uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms) {
 
 cudaError_t fused_launch(const FusedDesc &d, const float2 *in, float2 *out, uint64_t batch, const float2 *tw_a,
                          const float2 *tw_b, const float2 *tw_lo, const float2 *tw_hi, float in_im, float out_re,
-                         float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream) {
+                         float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream,
+                         const void *gtab) {
     FusedParams P;
     P.in = in;
     P.out = out;
@@ -65,6 +87,7 @@ cudaError_t fused_launch(const FusedDesc &d, const float2 *in, float2 *out, uint
     P.ctr = ctr;
     P.err = err;
     P.spin_limit = 1u << 22;  // ~0.5 s of 128 ns polls; a healthy wait is a few microseconds
+    P.gtab = (const uint4 *)gtab;
     const uint64_t grid = std::min<uint64_t>((uint64_t)P.nitems,
                                              (uint64_t)std::max(1, d.ctas_per_sm) * (uint64_t)std::max(1, sms));
     void *args[] = {(void *)&P};

@@ -216,31 +216,33 @@ __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_kernel(RagParams P,
     rag_loop(P, smem_rag, eng);
 }
 
-// Tensor-core split form.  Shared memory: the item region (FP32 exchange
-// tile + column twiddles, or a rows tile; the hi/lo A operands alias the
-// exchange tile while a tensor-core DFT runs), then the two G operand parts,
-// then the mbarrier.  TMEM (32 columns per 128 threads) is allocated once for
-// the CTA's whole run.
+// Tensor-core split forms.  Shared memory: the item region (FP32 exchange
+// tile + column twiddles, or a rows tile; the hi/lo A operands alias it while
+// a tensor-core DFT runs), then the two G operand parts, then the mbarrier.
+// TMEM (32 columns per 128 threads) is allocated once for the CTA's whole run.
+// `off_g` (the item region rounded up to 1 KB, or twice the A operand bytes
+// if larger) is passed by the host.
+template <int KIND>
 struct RagTcLayout {
     static constexpr int NMMA = kRagThreads / 128;
     static constexpr uint32_t TMEM_COLS = 128;
-    static constexpr size_t A_BYTES = (size_t)kRagThreads * kTcRowBytes;
+    static constexpr size_t A_BYTES = (size_t)kRagThreads * TcGeom<KIND>::ROW_BYTES;
     static_assert(NMMA * 32 <= (int)TMEM_COLS, "TMEM columns");
-    static_assert(2 * A_BYTES <= (size_t)kRagThreads * 16 * sizeof(float2), "A operands fit in the exchange tile");
 };
 
-template <bool BF16>
-__global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_tc_kernel(RagParams P, const uint4 *__restrict__ gtab,
-                                                                       uint32_t off_g) {
-    using Lay = RagTcLayout;
+template <int KIND>
+__global__ void __launch_bounds__(kRagThreads, (KIND == kTcTF32 ? 1 : 2))
+fft_ragged_tc_kernel(RagParams P, const uint4 *__restrict__ gtab, uint32_t off_g) {
+    using Lay = RagTcLayout<KIND>;
+    using Gm = TcGeom<KIND>;
     extern __shared__ __align__(1024) uint8_t smem_rtc[];
-    uint64_t *bar = (uint64_t *)(smem_rtc + off_g + 2 * kTcGBytes);
-    uint32_t *s_taddr = (uint32_t *)(smem_rtc + off_g + 2 * kTcGBytes + 8);
-    int *s_abort = (int *)(smem_rtc + off_g + 2 * kTcGBytes + 12);
+    uint64_t *bar = (uint64_t *)(smem_rtc + off_g + 2 * Gm::G_BYTES);
+    uint32_t *s_taddr = (uint32_t *)(smem_rtc + off_g + 2 * Gm::G_BYTES + 8);
+    int *s_abort = (int *)(smem_rtc + off_g + 2 * Gm::G_BYTES + 12);
     const int tid = threadIdx.x;
-    const uint4 *gsrc = gtab + (BF16 ? 2 : 0) * (kTcGBytes / 16);
+    const uint4 *gsrc = gtab + Gm::GTAB_OFF / 16;
     uint4 *gdst = (uint4 *)(smem_rtc + off_g);
-    for (int i = tid; i < 2 * kTcGBytes / 16; i += kRagThreads) gdst[i] = gsrc[i];
+    for (int i = tid; i < 2 * Gm::G_BYTES / 16; i += kRagThreads) gdst[i] = gsrc[i];
     if (tid < 32) tmem_alloc(s_taddr, Lay::TMEM_COLS);
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_tc_kernel(RagParams
     st.a_hi = smem_rtc;
     st.a_lo = smem_rtc + Lay::A_BYTES;
     st.g_hi = smem_rtc + off_g;
-    st.g_lo = smem_rtc + off_g + kTcGBytes;
+    st.g_lo = smem_rtc + off_g + Gm::G_BYTES;
     st.bar = bar;
     st.abort = s_abort;
     st.err = P.error;  // a completion wait that gives up stops the whole launch
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kRagThreads, 2) fft_ragged_tc_kernel(RagParams
     st.parity = 0;
     st.nmma = Lay::NMMA;
     st.spin_limit = kTcSpinLimit;
-    DftTc<BF16> eng{&st};
+    DftTc<KIND> eng{&st};
     rag_loop(P, (float2 *)smem_rtc, eng);
 
     tc_fence_before();
@@ -340,17 +342,27 @@ struct RaggedPlanImpl {
     void *gtab = nullptr;   // split form: the G operand parts (fft_passes_tc.cu)
 };
 
-static size_t rag_tc_off_g() { return (rag_smem_bytes() + 1023) & ~(size_t)1023; }
-static size_t rag_tc_smem_bytes() { return rag_tc_off_g() + 2 * kTcGBytes + 64; }
+static int rag_tc_kind(const RaggedPlanImpl &p) { return tc_kind_of_precision(p.precision); }
+static size_t rag_tc_a_bytes(int kind) {
+    return (size_t)kRagThreads * (kind == kTcTF32 ? TcGeom<kTcTF32>::ROW_BYTES : TcGeom<kTcF16>::ROW_BYTES);
+}
+static size_t rag_tc_off_g(const RaggedPlanImpl &p) {
+    return (std::max(rag_smem_bytes(), 2 * rag_tc_a_bytes(rag_tc_kind(p))) + 1023) & ~(size_t)1023;
+}
+static size_t rag_tc_smem_bytes(const RaggedPlanImpl &p) {
+    const size_t g = rag_tc_kind(p) == kTcTF32 ? TcGeom<kTcTF32>::G_BYTES : TcGeom<kTcF16>::G_BYTES;
+    return rag_tc_off_g(p) + 2 * g + 64;
+}
 static const void *rag_kernel(const RaggedPlanImpl &p) {
     switch (p.precision) {
-        case GBFFT_PREC_TC_FP16: return (const void *)fft_ragged_tc_kernel<false>;
-        case GBFFT_PREC_TC_BF16X3: return (const void *)fft_ragged_tc_kernel<true>;
+        case GBFFT_PREC_TC_FP16: return (const void *)fft_ragged_tc_kernel<kTcF16>;
+        case GBFFT_PREC_TC_BF16X3: return (const void *)fft_ragged_tc_kernel<kTcBF16>;
+        case GBFFT_PREC_TC_TF32: return (const void *)fft_ragged_tc_kernel<kTcTF32>;
         default: return (const void *)fft_ragged_kernel;
     }
 }
 static size_t rag_kernel_smem(const RaggedPlanImpl &p) {
-    return p.precision == GBFFT_PREC_FP32 ? rag_smem_bytes() : rag_tc_smem_bytes();
+    return p.precision == GBFFT_PREC_FP32 ? rag_smem_bytes() : rag_tc_smem_bytes(p);
 }
 
 static void build_items(RaggedPlanImpl &p) {
@@ -575,9 +587,12 @@ static cudaError_t rag_enqueue(RaggedPlanImpl &p, const void *in, void *out, cud
     if (e != cudaSuccess) return e;
     RagParams P = rag_params(p, in, out);
     if (p.nitems > 0) {
-        const unsigned grid = (unsigned)std::max(1, std::min<int>(2 * p.sms, (int)p.nitems));
+        // two resident CTAs per SM, one for the TF32 split form (its A operands
+        // take twice the shared memory)
+        const int per_sm = p.precision == GBFFT_PREC_TC_TF32 ? 1 : 2;
+        const unsigned grid = (unsigned)std::max(1, std::min<int>(per_sm * p.sms, (int)p.nitems));
         const uint4 *gtab = (const uint4 *)p.gtab;
-        uint32_t off_g = (uint32_t)rag_tc_off_g();
+        uint32_t off_g = (uint32_t)rag_tc_off_g(p);
         void *args[] = {(void *)&P, (void *)&gtab, (void *)&off_g};
         e = cudaLaunchKernel(rag_kernel(p), dim3(grid), dim3(kRagThreads), args, rag_kernel_smem(p), s);
         if (e != cudaSuccess) return e;

@@ -1,4 +1,4 @@
-// Tensor-core (tcgen05) 16-point DFTs for the split-precision form.
+// Tensor-core (tcgen05) 16-point DFTs for the split-precision forms.
 //
 // Every thread of a tile owns one 16-point vector x (the E = 16 samples of a
 // radix-16 sub-pass).  A whole sub-pass is then one real matrix product per
@@ -9,18 +9,26 @@
 //     G[e][16+q]   = -sin(2 pi q e / 16)   G[16+e][16+q] = cos(2 pi q e / 16)
 // so that D's row r = [Re X_0..15 | Im X_0..15], the forward DFT of x.
 //
-// Precision: A and G are split into 16-bit hi + lo parts (FP16 or BF16) and
+// Precision: A and G are split into hi + lo parts and
 // D = Ah.Gh + Ah.Gl + Al.Gh is accumulated in FP32 in tensor memory (the
-// Al.Gl term is below the FP32 rounding of the result).  Each row is first
-// scaled by an exact power of two so that its largest component lies in
-// [1, 2): FP16's range then always suffices and hi + lo carry 22 significant
-// bits (BF16: 16 bits).
+// Al.Gl term is below the FP32 rounding of the result).  Three operand kinds:
+//   FP16 / BF16 (kind::f16): each row is first scaled by an exact power of two
+//     so that its largest component lies in [1, 2); FP16's range then always
+//     suffices and hi + lo carry 22 significant bits (BF16: 16 bits).
+//   TF32 (kind::tf32): hi = x rounded to the nearest TF32 value (an integer
+//     add and mask), lo = x - hi (exact in FP32; the tensor core uses its top
+//     11 significant bits).  TF32 keeps FP32's exponent range, so no scaling
+//     is needed: three instructions per value instead of the 16-bit forms'
+//     scale, convert, convert back, subtract and convert.  About 22
+//     significant bits.
 //
 // Operands live in shared memory in the canonical K-major, no-swizzle layout
-// of the tcgen05 matrix descriptors: 8 x 8 16-bit core matrices of 128 bytes,
-// core matrix (row block i, K block j) at (i * 4 + j) * 128 bytes, so the
-// descriptor's leading-dimension offset (between K-adjacent core matrices) is
-// 128 bytes and its stride-dimension offset (between row-adjacent ones) 512.
+// of the tcgen05 matrix descriptors: core matrices of 8 rows x 16 bytes (8
+// 16-bit or 4 32-bit values), row r's K-block j of a 32-value row at
+// ((r / 8) * KB + j) * 128 + (r % 8) * 16 bytes with KB = 4 K-blocks (16-bit)
+// or 8 (TF32) per row block, so the descriptor's leading-dimension offset
+// (between K-adjacent core matrices) is 128 bytes and its stride-dimension
+// offset (between row-adjacent ones) KB * 128.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -30,36 +38,52 @@
 
 namespace gbfft {
 
-constexpr int kTcRowBytes = 64;        // 32 16-bit values
-constexpr uint32_t kTcLbo = 128;       // bytes between K-adjacent core matrices
-constexpr uint32_t kTcSbo = 512;       // bytes between row-adjacent core matrices
-constexpr int kTcGBytes = 32 * kTcRowBytes;  // one 32 x 32 G part
+// Operand kinds of the split forms.
+enum : int { kTcF16 = 0, kTcBF16 = 1, kTcTF32 = 2 };
+
+constexpr uint32_t kTcLbo = 128;  // bytes between K-adjacent core matrices
+
+// Geometry of one operand kind: 32 values per operand row.
+template <int KIND>
+struct TcGeom {
+    static constexpr int ELEM = KIND == kTcTF32 ? 4 : 2;  // bytes per value
+    static constexpr int ROW_BYTES = 32 * ELEM;            // one A row
+    static constexpr int KB = ROW_BYTES / 16;              // K-blocks (core matrices) per row block
+    static constexpr uint32_t SBO = KB * 128u;             // bytes between row-adjacent core matrices
+    static constexpr int G_BYTES = 32 * ROW_BYTES;         // one 32 x 32 G part (hi or lo)
+    static constexpr int NKSTEP = ROW_BYTES / 32;          // MMAs along K (32 bytes of K each)
+    // byte offset of the kind's [hi | lo] parts in the G table
+    static constexpr int GTAB_OFF = KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 4096 : 8192);
+    // Instruction descriptor: D F32, A/B F16 (0) / BF16 (1) under kind::f16 or
+    // TF32 (2) under kind::tf32, both K-major, M = 128, N = 32.
+    static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 1 : 2)) << 7) |
+                                      ((uint32_t)(KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 1 : 2)) << 10) |
+                                      ((32u >> 3) << 17) | ((128u >> 4) << 24);
+    // Byte offset of value (row, k) of a K-major no-swizzle operand.
+    __host__ __device__ static constexpr uint32_t elem_offset(uint32_t row, uint32_t k) {
+        return ((row >> 3) * KB + ((k * ELEM) >> 4)) * 128u + (row & 7) * 16u + ((k * ELEM) & 15u);
+    }
+};
+
+// 16-bit kinds (unchanged users of the older names)
+constexpr int kTcRowBytes = TcGeom<kTcF16>::ROW_BYTES;
+constexpr int kTcGBytes = TcGeom<kTcF16>::G_BYTES;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// Byte offset of element (row, k) in a K-major no-swizzle operand with 32 K.
+// Byte offset of element (row, k) in a 16-bit K-major no-swizzle operand.
 __host__ __device__ __forceinline__ uint32_t tc_elem_offset(uint32_t row, uint32_t k) {
-    return ((row >> 3) * 4 + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2;
+    return TcGeom<kTcF16>::elem_offset(row, k);
 }
 
 // tcgen05 shared-memory matrix descriptor (no swizzle, K-major).
-__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr) {
+__device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr, uint32_t sbo) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFF) >> 4);        // bits 0-13: start address / 16
     d |= (uint64_t)(kTcLbo >> 4) << 16;             // bits 16-29: leading-dimension byte offset / 16
-    d |= (uint64_t)(kTcSbo >> 4) << 32;             // bits 32-45: stride-dimension byte offset / 16
+    d |= (uint64_t)(sbo >> 4) << 32;                // bits 32-45: stride-dimension byte offset / 16
     d |= (uint64_t)1 << 46;                         // bits 46-47: descriptor version 1
     return d;                                       // base offset 0, swizzle mode 0 (none)
-}
-
-// Instruction descriptor, kind::f16: D F32, A/B F16 (bf16 = false) or BF16,
-// both K-major, M = 128, N = 32.
-__host__ __device__ constexpr uint32_t tc_idesc(bool bf16) {
-    return (1u << 4)                          // D format: F32
-           | ((bf16 ? 1u : 0u) << 7)          // A format
-           | ((bf16 ? 1u : 0u) << 10)         // B format
-           | ((32u >> 3) << 17)               // N / 8
-           | ((128u >> 4) << 24);             // M / 16
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -92,14 +116,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
+template <int KIND>
 __device__ __forceinline__ void tc_mma(uint32_t d_taddr, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                        uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.u32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
+    if constexpr (KIND == kTcTF32) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.u32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.u32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_taddr),
+            "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+            : "memory");
+    }
 }
 __device__ __forceinline__ void tc_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -138,9 +172,20 @@ struct TcSplit {
     }
 };
 
+// TF32 split: hi = x rounded to the nearest TF32 value (sign, exponent and 10
+// explicit mantissa bits; ties away from zero), lo = x - hi, exact in FP32 and
+// of either sign, |lo| <= 2^-11 |x|.  Rounding (rather than clearing the low
+// bits) halves lo and, more importantly, makes the error of the tensor core's
+// reduction of lo to TF32 unbiased: with truncation every lo shares x's sign
+// and the dropped bits pile up coherently through the stages.
+__device__ __forceinline__ void tc_split_tf32(float x, uint32_t &hi, uint32_t &lo) {
+    hi = (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u;
+    lo = __float_as_uint(x - __uint_as_float(hi));
+}
+
 // Per-CTA state of the tensor-core DFT.
 struct TcState {
-    uint8_t *a_hi;       // [threads rows][32] 16-bit, canonical layout
+    uint8_t *a_hi;       // [threads rows][32 values], canonical layout
     uint8_t *a_lo;
     const uint8_t *g_hi; // [32][32]
     const uint8_t *g_lo;
@@ -155,42 +200,63 @@ struct TcState {
 
 // Forward 16-point DFT of x (natural order in, natural order out) on the
 // tensor cores.  Must be called by all threads of the CTA at the same point.
-template <bool BF16>
+template <int KIND>
 __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
+    using Gm = TcGeom<KIND>;
     const uint32_t r = threadIdx.x;
-    // 1. exact power-of-two scaling: largest |component| to [1, 2)
-    float m = 0.f;
+    float up = 1.f;
+    if constexpr (KIND == kTcTF32) {
+        // A shares its bytes with the FP32 exchange tile: every thread must
+        // have finished reading its exchange inputs before any thread writes A.
+        __syncthreads();
 #pragma unroll
-    for (int e = 0; e < 16; ++e) m = fmaxf(m, fmaxf(fabsf(x[e].x), fabsf(x[e].y)));
-    int ex = 0;
-    if (m > 0.f) {
-        ex = (int)((__float_as_uint(m) >> 23) & 0xff) - 127;
-        ex = ex < -126 ? -126 : ex;
-    }
-    ex = ex > 126 ? 126 : ex;
-    const float down = __uint_as_float((uint32_t)(127 - ex) << 23);  // 2^-ex (ex in [-126, 126])
-    // A shares its bytes with the FP32 exchange tile: every thread must have
-    // finished reading its exchange inputs before any thread writes A.
-    __syncthreads();
-    // 2. split into hi/lo rows of A
-    uint32_t hi[16], lo[16];
+        for (int kb = 0; kb < 8; ++kb) {  // 8 chunks of 4 K-values (16 bytes)
+            uint32_t h[4], l[4];
 #pragma unroll
-    for (int e = 0; e < 16; e += 2) {
-        uint16_t h0, l0, h1, l1;
-        TcSplit<BF16>::split(x[e].x * down, h0, l0);
-        TcSplit<BF16>::split(x[e + 1].x * down, h1, l1);
-        hi[e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        lo[e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-        TcSplit<BF16>::split(x[e].y * down, h0, l0);
-        TcSplit<BF16>::split(x[e + 1].y * down, h1, l1);
-        hi[8 + e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-        lo[8 + e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-    }
+            for (int i = 0; i < 4; ++i) {
+                const int k = 4 * kb + i;
+                tc_split_tf32(k < 16 ? x[k].x : x[k - 16].y, h[i], l[i]);
+            }
+            const uint32_t off = Gm::elem_offset(r, 4 * kb);
+            *(uint4 *)(s.a_hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
+            *(uint4 *)(s.a_lo + off) = make_uint4(l[0], l[1], l[2], l[3]);
+        }
+    } else {
+        constexpr bool BF16 = KIND == kTcBF16;
+        // 1. exact power-of-two scaling: largest |component| to [1, 2)
+        float m = 0.f;
 #pragma unroll
-    for (int kb = 0; kb < 4; ++kb) {  // 4 chunks of 8 K-values (16 bytes)
-        const uint32_t off = tc_elem_offset(r, kb * 8);
-        *(uint4 *)(s.a_hi + off) = make_uint4(hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
-        *(uint4 *)(s.a_lo + off) = make_uint4(lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+        for (int e = 0; e < 16; ++e) m = fmaxf(m, fmaxf(fabsf(x[e].x), fabsf(x[e].y)));
+        int ex = 0;
+        if (m > 0.f) {
+            ex = (int)((__float_as_uint(m) >> 23) & 0xff) - 127;
+            ex = ex < -126 ? -126 : ex;
+        }
+        ex = ex > 126 ? 126 : ex;
+        const float down = __uint_as_float((uint32_t)(127 - ex) << 23);  // 2^-ex (ex in [-126, 126])
+        up = __uint_as_float((uint32_t)(127 + ex) << 23);                // 2^ex
+        // A shares its bytes with the FP32 exchange tile (see above).
+        __syncthreads();
+        // 2. split into hi/lo rows of A
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int e = 0; e < 16; e += 2) {
+            uint16_t h0, l0, h1, l1;
+            TcSplit<BF16>::split(x[e].x * down, h0, l0);
+            TcSplit<BF16>::split(x[e + 1].x * down, h1, l1);
+            hi[e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+            lo[e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+            TcSplit<BF16>::split(x[e].y * down, h0, l0);
+            TcSplit<BF16>::split(x[e + 1].y * down, h1, l1);
+            hi[8 + e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
+            lo[8 + e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+        }
+#pragma unroll
+        for (int kb = 0; kb < 4; ++kb) {  // 4 chunks of 8 K-values (16 bytes)
+            const uint32_t off = Gm::elem_offset(r, kb * 8);
+            *(uint4 *)(s.a_hi + off) = make_uint4(hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
+            *(uint4 *)(s.a_lo + off) = make_uint4(lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+        }
     }
     fence_proxy_async_smem();  // generic-proxy writes -> visible to the tensor core
     tc_fence_before();
@@ -201,20 +267,20 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
         if (*(volatile uint32_t *)s.err != 0u) *s.abort = 1;
         if (!*s.abort) {
             tc_fence_after();
-            constexpr uint32_t idesc = tc_idesc(BF16);
             const uint32_t ah = smem_u32(s.a_hi), al = smem_u32(s.a_lo);
             const uint32_t gh = smem_u32(s.g_hi), gl = smem_u32(s.g_lo);
             for (uint32_t mb = 0; mb < s.nmma; ++mb) {
                 const uint32_t d = s.taddr + mb * 32;
-                const uint32_t arow = mb * 128 * kTcRowBytes;  // 128 rows = 16 row blocks of 512 B
+                const uint32_t arow = mb * 128 * Gm::ROW_BYTES;  // 128 rows = 16 row blocks
                 uint32_t acc = 0;
 #pragma unroll
                 for (int part = 0; part < 3; ++part) {
                     const uint32_t a = (part == 2 ? al : ah) + arow;
                     const uint32_t g = part == 1 ? gl : gh;
 #pragma unroll
-                    for (uint32_t ks = 0; ks < 2; ++ks) {  // K = 32 = 2 x 16
-                        tc_mma(d, tc_smem_desc(a + ks * 2 * kTcLbo), tc_smem_desc(g + ks * 2 * kTcLbo), idesc, acc);
+                    for (uint32_t ks = 0; ks < (uint32_t)Gm::NKSTEP; ++ks) {  // 32 bytes of K per MMA
+                        tc_mma<KIND>(d, tc_smem_desc(a + ks * 2 * kTcLbo, Gm::SBO),
+                                     tc_smem_desc(g + ks * 2 * kTcLbo, Gm::SBO), Gm::IDESC, acc);
                         acc = 1;
                     }
                 }
@@ -238,22 +304,31 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
     const uint32_t taddr = s.taddr + ((((r >> 5) & 3) * 32) << 16) + (r >> 7) * 32;
     tmem_ld32(taddr, d);
     tc_fence_before();
-    const float up = __uint_as_float((uint32_t)(127 + ex) << 23);  // 2^ex
+    if constexpr (KIND == kTcTF32) {
 #pragma unroll
-    for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]) * up, __uint_as_float(d[16 + q]) * up);
+        for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]), __uint_as_float(d[16 + q]));
+    } else {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]) * up, __uint_as_float(d[16 + q]) * up);
+    }
 }
 
 // Butterfly engine for pass_tile / rows_tile: radix-16 butterflies on the
 // tensor cores, the radix 2/4/8 remainder on the FP32 pipes.
-template <bool BF16>
+template <int KIND>
 struct DftTc {
     TcState *s;
     template <int R>
     __device__ __forceinline__ void run(float2 (&x)[R]) {
-        if constexpr (R == 16) tc_dft16<BF16>(x, *s);
+        if constexpr (R == 16) tc_dft16<KIND>(x, *s);
         else Dft<R>::run(x);
     }
 };
+
+// gbfft_precision value -> operand kind
+__host__ __device__ constexpr int tc_kind_of_precision(int precision) {
+    return precision == 2 ? kTcBF16 : (precision == 3 ? kTcTF32 : kTcF16);
+}
 
 constexpr uint32_t kTcSpinLimit = 1u << 20;  // polls of an MMA completion that takes microseconds
 

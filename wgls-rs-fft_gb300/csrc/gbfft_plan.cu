@@ -100,7 +100,8 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         bool dup = false;
         for (const PlanVariant &v : c) dup |= split_passes(logn, v.max_logr) == parts;
         if (dup || parts[0] < 5) continue;
-        if (!tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd))
+        if (parts.size() == 2 && (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, fd)
+                                     : fused2_kernel_info(parts[0], parts[1], fd)))
             c.push_back(PlanVariant{m, false, true});
         c.push_back(PlanVariant{m, false});
         if (!tc) c.push_back(PlanVariant{m, true});
@@ -146,7 +147,7 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         int logp = 0;
         for (size_t i = 0; i < parts.size(); ++i) {
             PassDesc d;
-            const bool ok = tc ? pass_tc_kernel_info(parts[i], i == 0, precision == GBFFT_PREC_TC_BF16X3, d)
+            const bool ok = tc ? pass_tc_kernel_info(parts[i], i == 0, precision, d)
                                : pass_kernel_info(parts[i], i == 0, d);
             if (!ok) {
                 why = std::string("no ") + (tc ? "tensor-core " : "") + "pass kernel for radix 2^" +
@@ -162,7 +163,9 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
             p.passes.push_back(d);
         }
         p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
-        if (fused3 || (v.fused && !tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], p.fused))) {
+        if (fused3 || (v.fused && parts.size() == 2 &&
+                       (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, p.fused)
+                           : fused2_kernel_info(parts[0], parts[1], p.fused)))) {
             if ((e = fused_prepare(p.fused)) != cudaSuccess) {
                 why = cudaGetErrorString(e);
                 return GBFFT_ERR_CUDA;
@@ -239,7 +242,8 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
         e = fused_launch(p.fused, pair_in, out, batch, p.tw + p.passes[a].sub_tw_offset,
                          p.tw + p.passes[a + 1].sub_tw_offset, p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset,
                          (inv && !pair3) ? -1.0f : 1.0f, scale, inv ? -scale : 1.0f,
-                         pair3 ? LoadOps{nullptr, 0u, 0.f, 0u} : ops, (uint32_t *)ctr->ptr, err, p.sms, stream);
+                         pair3 ? LoadOps{nullptr, 0u, 0.f, 0u} : ops, (uint32_t *)ctr->ptr, err, p.sms, stream,
+                         p.gtab);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;

@@ -51,6 +51,7 @@ struct FusedDesc {
     uint32_t tiles_per_group = 0;  // of each pass
     uint64_t group_samples = 0;
     int ctas_per_sm = 0;
+    int tmem_cols = 0;  // split forms: TMEM columns a CTA holds (bounds the CTAs per SM)
 };
 // Upper bound on the intermediates in flight between the two passes (bytes).
 constexpr uint64_t kFusedWindowBytes = 48ull << 20;
@@ -105,13 +106,16 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
                         bool persistent = false, int sms = 0, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 
 // fft_passes_tc.cu (split-precision tensor-core form)
-bool pass_tc_kernel_info(int logr, bool first, bool bf16, PassDesc &d);
+bool pass_tc_kernel_info(int logr, bool first, int precision, PassDesc &d);
+// both passes of a two-pass transform in one persistent launch (radices 2^8/2^7 .. 2^9/2^9)
+bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d);
 cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                            const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, const void *gtab,
                            uint32_t *err, cudaStream_t stream, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
-constexpr size_t kTcGtabBytes = 4 * 2048;
+// G table: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (2 KB each), [TF32 hi | TF32 lo] (4 KB each)
+constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096;
 
 // fft_fused2.cu, fft_fused3.cu
 bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d);
@@ -120,7 +124,8 @@ cudaError_t fused_prepare(FusedDesc &d);
 uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms);
 cudaError_t fused_launch(const FusedDesc &d, const float2 *in, float2 *out, uint64_t batch, const float2 *tw_a,
                          const float2 *tw_b, const float2 *tw_lo, const float2 *tw_hi, float in_im, float out_re,
-                         float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream);
+                         float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream,
+                         const void *gtab = nullptr);
 
 // log2 radices (each <= max_logr) of the global passes for a multi-pass
 // transform of 2^logn.

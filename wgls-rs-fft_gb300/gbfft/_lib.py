@@ -18,6 +18,7 @@ INVERSE = +1
 PREC_FP32 = 0
 PREC_TC_FP16 = 1
 PREC_TC_BF16X3 = 2
+PREC_TC_TF32 = 3
 WINDOW_NONE = 0
 WINDOW_HANN = 1
 

@@ -95,12 +95,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profile_traffic(workload: str):
+def profile_traffic(workload: str, precision: str = "fp32"):
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu
-    summary (line 'traffic_bytes_per_launch: <int>'), else None."""
-    path = os.path.join(ROOT, "profiles", f"fft_{workload}.md")
+    summary (line 'traffic_bytes_per_launch: <int>') of the workload in this
+    precision (profiles/fft_<workload>_<precision>.md; the FP32 form's file
+    has no suffix), else None."""
+    name = f"fft_{workload}.md" if precision == "fp32" else f"fft_{workload}_{precision}.md"
     try:
-        for line in open(path):
+        for line in open(os.path.join(ROOT, "profiles", name)):
             if line.strip().startswith("traffic_bytes_per_launch:"):
                 return int(float(line.split(":", 1)[1].strip()))
     except OSError:
@@ -362,7 +364,7 @@ def run_ragged(args, ctx, dev, rank, world):
                        "l2": "inputs (4 GB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,
-                         "traffic": profile_traffic("ragged_c5") if args.ragged_count == 10000 else None,
+                         "traffic": profile_traffic("ragged_c5", args.precision) if args.ragged_count == 10000 else None,
                          "peak_source": peak_kind,
                          "alg_bytes_per_launch": alg_bytes, "executed_bytes_per_launch": exec_bytes,
                          "launch_us": ms * 1e3 / max(1, launches)},
@@ -473,7 +475,7 @@ def main():
     achieved = alg_bytes / launch_s / 1e9
     floor_achieved = 16 * n * batch / (launch_s * launches_per_transform) / 1e9
     peak, peak_kind = peaks()
-    traffic = profile_traffic(workload)
+    traffic = profile_traffic(workload, args.precision)
 
     # check the last step's roundtrip (cheap, catches a broken build), and the
     # forward result of a few rows against a float64 FFT of the same rows

@@ -65,3 +65,54 @@ def test_leaderboard_rivals_pass_on_gpu(lib_built, capsys):
                 assert res.msamples_per_sec > 0
     assert lb.main(["--sizes", "256"]) == 0
     assert "RIVALRY LEADERBOARD" in capsys.readouterr().out
+
+
+NCU_CSV = '''==PROF== Connected to process 1
+"ID","Process ID","Process Name","Host Name","Kernel Name","Context","Stream","Block Size","Grid Size","Device","CC","Section Name","Metric Name","Metric Unit","Metric Value"
+"0","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","dram__bytes_read.sum","byte","8,388,608"
+"0","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","dram__bytes_write.sum","byte","8388608"
+"0","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","gpu__time_duration.sum","ns","4000"
+"1","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","dram__bytes_read.sum","byte","8388608"
+"1","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","dram__bytes_write.sum","byte","8388608"
+"1","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","gpu__time_duration.sum","us","6"
+"2","7","python3.12","h","void gbfft::twiddle_fill_kernel(float2 *)","1","7","(256, 1, 1)","(4, 1, 1)","0","10.3","Command line profiler metrics","gpu__time_duration.sum","ns","1500"
+'''
+
+
+def test_parse_ncu_csv_aggregates_per_kernel(lib_built):
+    from gbfft import leaderboard as lb
+    ks = lb.parse_ncu_csv(NCU_CSV)
+    assert [k.kernel for k in ks] == ["gbfft::fft_rows_kernel<10, 11>", "gbfft::twiddle_fill_kernel"]
+    rows = ks[0]
+    assert rows.launches == 2 and rows.seconds == pytest.approx(10e-6) and rows.dram_bytes == 4 * 8388608
+    assert ks[1].launches == 1 and ks[1].dram_bytes == 0
+    assert lb.parse_ncu_csv("no csv here") == []
+    text = lb.format_counters(1024, 1024, "GB300 FP32", ks)
+    assert "2 launch" not in text and "3 launch(es)" in text and "fft_rows_kernel" in text
+
+
+def test_ncu_counters_runs_plain_first_then_ncu(lib_built, tmp_path):
+    """The capture runs only after the same child command exited 0 without
+    ncu; a failing plain run raises before ncu is started."""
+    from gbfft import leaderboard as lb
+    calls = []
+
+    class R:
+        def __init__(self, rc):
+            self.returncode, self.stderr, self.stdout = rc, "", ""
+
+    def fake_run(cmd, **kw):
+        calls.append(cmd)
+        if cmd[0] == "ncu":
+            log = cmd[cmd.index("--log-file") + 1]
+            with open(log, "w") as f:
+                f.write(NCU_CSV)
+            assert "--clock-control" in cmd and cmd[cmd.index("--clock-control") + 1] == "none"
+        return R(0)
+
+    ks = lb.ncu_counters(1024, 0, run=fake_run)
+    assert len(calls) == 2 and calls[0][0] != "ncu" and calls[1][0] == "ncu"
+    assert calls[1][calls[1].index("--metrics") + 1] == ",".join(lb.NCU_METRICS)
+    assert ks[0].launches == 2
+    with pytest.raises(RuntimeError):
+        lb.ncu_counters(1024, 0, run=lambda cmd, **kw: R(1))

@@ -21,19 +21,32 @@ Rivals:
     (the reference's cuFFT wrapper plans batch = 1 and loops,
     src/cufft_wrapper.rs:49-54)
 
-Run:  python -m gbfft.leaderboard [--sizes 256 1024 ...]
+With --ncu, each size is followed by the device-side counters of the GB300
+rivals: the rival's transform of the same batch is run once plainly and then
+once under Nsight Compute (launch-list metrics only: device time and DRAM
+bytes of every kernel inside an NVTX range), and each kernel's launches, time,
+DRAM traffic and achieved DRAM bandwidth are printed beside the algorithmic
+traffic (16 bytes per sample per pass, 1 pass up to N = 2^14, 2 above).
+
+Run:  python -m gbfft.leaderboard [--sizes 256 1024 ...] [--ncu]
 """
 from __future__ import annotations
 
 import argparse
+import csv
+import io
 import math
+import os
+import subprocess
+import sys
+import tempfile
 import time
 from dataclasses import dataclass
 from typing import Callable, List, Optional, Sequence
 
 import numpy as np
 
-from ._lib import PREC_TC_FP16, GbfftError, status_string
+from ._lib import PREC_FP32, PREC_TC_FP16, GbfftError, status_string
 from .gpu_fft import FftExecutor, GpuFft
 
 MAX_TOTAL_SAMPLES = 16 * 1024 * 1024  # src/benchmark.rs:47
@@ -172,16 +185,122 @@ def format_table(n: int, results: Sequence[Result]) -> str:
     return "\n".join(lines)
 
 
+# ---- device-side counters (Nsight Compute) ---------------------------------
+
+NCU_METRICS = ("gpu__time_duration.sum", "dram__bytes_read.sum", "dram__bytes_write.sum")
+NCU_RANGE = "gbfft_measure"
+
+
+@dataclass
+class KernelCounters:
+    kernel: str
+    launches: int
+    seconds: float
+    dram_bytes: float
+
+
+def _number(text: str) -> float:
+    return float(text.replace(",", "").strip() or "nan")
+
+
+def parse_ncu_csv(text: str) -> List[KernelCounters]:
+    """Per-kernel totals from `ncu --csv --print-units base` output (one row
+    per launch and metric; lines before the CSV header are skipped)."""
+    lines = text.splitlines()
+    start = next((i for i, l in enumerate(lines) if l.startswith('"ID"')), None)
+    if start is None:
+        return []
+    time_scale = {"ns": 1e-9, "nsecond": 1e-9, "us": 1e-6, "usecond": 1e-6, "ms": 1e-3, "msecond": 1e-3,
+                  "s": 1.0, "second": 1.0}
+    byte_scale = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9}
+    per_launch = {}  # (launch ID, kernel) -> {metric: value in seconds or bytes}
+    for row in csv.DictReader(io.StringIO("\n".join(lines[start:]))):
+        metric, unit = row["Metric Name"], row.get("Metric Unit", "")
+        if metric not in NCU_METRICS:
+            continue
+        value = _number(row["Metric Value"])
+        value *= time_scale.get(unit, 1e-9) if metric == "gpu__time_duration.sum" else byte_scale.get(unit, 1.0)
+        per_launch.setdefault((row["ID"], row["Kernel Name"]), {})[metric] = value
+    out = {}
+    for (_, name), rec in per_launch.items():
+        short = name.split("(")[0].replace("void ", "").strip()
+        k = out.setdefault(short, KernelCounters(short, 0, 0.0, 0.0))
+        k.launches += 1
+        k.seconds += rec.get("gpu__time_duration.sum", 0.0)
+        k.dram_bytes += rec.get("dram__bytes_read.sum", 0.0) + rec.get("dram__bytes_write.sum", 0.0)
+    return sorted(out.values(), key=lambda k: -k.seconds)
+
+
+def ncu_child(n: int, precision: int) -> int:
+    """Body of the profiled process: one untimed transform of the size's
+    batch, then one inside the NVTX range the capture is limited to."""
+    rival = SplitFormGpuFft() if precision == PREC_TC_FP16 else GpuFft()
+    inputs = pipeline_input(n, choose_batch_size(n))
+    rival.fft(inputs)
+    import torch
+    torch.cuda.nvtx.range_push(NCU_RANGE)
+    rival.fft(inputs)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    return 0
+
+
+def ncu_counters(n: int, precision: int, ncu: str = "ncu", run=subprocess.run) -> List[KernelCounters]:
+    """Run the size's transform plainly, then (only if that exited 0) under
+    ncu with the launch-list metrics, and return the per-kernel counters."""
+    child = [sys.executable, "-m", "gbfft.leaderboard", "--ncu-child", str(n), "--precision", str(precision)]
+    env = dict(os.environ)
+    pkg_parent = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env["PYTHONPATH"] = pkg_parent + os.pathsep + env.get("PYTHONPATH", "")
+    plain = run(child, env=env, capture_output=True, text=True)
+    if plain.returncode != 0:
+        raise RuntimeError(f"plain run failed ({plain.returncode}): {plain.stderr[-400:]}")
+    with tempfile.TemporaryDirectory() as d:
+        log = os.path.join(d, "launches.csv")
+        cmd = [ncu, "--metrics", ",".join(NCU_METRICS), "--clock-control", "none", "--nvtx", "--nvtx-include",
+               f"{NCU_RANGE}/", "--print-units", "base", "--csv", "--log-file", log, *child]
+        r = run(cmd, env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"ncu failed ({r.returncode}): {r.stderr[-400:]}")
+        with open(log) as f:
+            return parse_ncu_csv(f.read())
+
+
+def format_counters(n: int, batch: int, label: str, counters: Sequence[KernelCounters]) -> str:
+    passes = 1 if n <= 1 << 14 else 2
+    alg = 16.0 * n * batch * passes
+    total_t = sum(k.seconds for k in counters)
+    lines = [f"  ncu, {label}: {sum(k.launches for k in counters)} launch(es), {total_t * 1e6:.1f} us on the device; "
+             f"algorithmic traffic {alg / 1e6:.1f} MB ({passes} pass(es) x 16 B/sample) = "
+             f"{(alg / total_t / 1e9) if total_t > 0 else float('nan'):.0f} GB/s"]
+    for k in counters:
+        bw = k.dram_bytes / k.seconds / 1e9 if k.seconds > 0 else float("nan")
+        lines.append(f"    {k.kernel:<48} x{k.launches:<3} {k.seconds * 1e6:>10.1f} us  DRAM {k.dram_bytes / 1e6:>9.1f} MB"
+                     f"  {bw:>7.0f} GB/s")
+    return "\n".join(lines)
+
+
 def main(argv: Optional[Sequence[str]] = None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--sizes", type=int, nargs="*", default=list(FFT_SIZES))
+    ap.add_argument("--ncu", action="store_true", help="print Nsight Compute counters of the GB300 rivals")
+    ap.add_argument("--ncu-path", default="ncu")
+    ap.add_argument("--ncu-child", type=int, default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--precision", type=int, default=PREC_FP32, help=argparse.SUPPRESS)
     args = ap.parse_args(argv)
+    if args.ncu_child is not None:
+        return ncu_child(args.ncu_child, args.precision)
     print("\n=== GB300 FFT RIVALRY LEADERBOARD ===")
     print("Measuring complete GPU pipeline performance (host-to-device + GPU compute + device-to-host)")
     rivals = default_rivals()
     for n in args.sizes:
         batch = choose_batch_size(n)
         print(format_table(n, [run_rival(r, n, batch) for r in rivals]))
+        if args.ncu:
+            for prec, label in ((PREC_FP32, "GB300 FP32"), (PREC_TC_FP16, "GB300 split FP16")):
+                if prec == PREC_TC_FP16 and n < 1 << 15:
+                    continue
+                print(format_counters(n, batch, label, ncu_counters(n, prec, args.ncu_path)))
     return 0
 
 

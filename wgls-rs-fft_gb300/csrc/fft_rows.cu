@@ -37,7 +37,9 @@ struct RowsCfg : SubCfg<LOGN> {
     static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * S::N * sizeof(float2) : 0;
 };
 
-template <int LOGN, int LOGS>
+// DIRC: -1 forward, +1 inverse (a launch has one direction, so the sign and
+// scale work is resolved at compile time).
+template <int LOGN, int LOGS, int DIRC>
 __global__ void __launch_bounds__(RowsCfg<LOGN, LOGS>::THREADS, RowsCfg<LOGN, LOGS>::MINB)
 fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                 float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
@@ -48,7 +50,7 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
         return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
                       (uint32_t)row};
     };
-    rows_tile<LOGN, C::G>(ref, tw, smem_rows, ops);
+    rows_tile<LOGN, C::G, DIRC>(ref, tw, smem_rows, ops);
 }
 
 // Persistent variant for the sizes whose per-transform footprint allows only
@@ -56,7 +58,7 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
 // blockIdx.x, +gridDim.x, ... and, before computing a tile, asks L2 for the
 // next one (one 128-byte line per thread), so the HBM fetch of tile i+1
 // overlaps the shared-memory sub-passes of tile i.
-template <int LOGN, int LOGS>
+template <int LOGN, int LOGS, int DIRC>
 __global__ void __launch_bounds__(RowsCfg<LOGN, LOGS>::THREADS, RowsCfg<LOGN, LOGS>::MINB)
 fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                            float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
@@ -77,7 +79,7 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
             return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
                       (uint32_t)row};
         };
-        rows_tile<LOGN, C::G>(ref, tw, smem_rows, ops);
+        rows_tile<LOGN, C::G, DIRC>(ref, tw, smem_rows, ops);
         __syncthreads();  // shared memory is reused by the next tile
     }
 }
@@ -89,8 +91,10 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
 template <int LOGN, int LOGS = 12>
 static void rows_describe(RowsKernelInfo &k) {
     using C = RowsCfg<LOGN, LOGS>;
-    k.fn = (const void *)fft_rows_kernel<LOGN, LOGS>;
-    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN, LOGS>;
+    k.fn = (const void *)fft_rows_kernel<LOGN, LOGS, -1>;
+    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, -1>;
+    k.fn_inv = (const void *)fft_rows_kernel<LOGN, LOGS, 1>;
+    k.fn_persistent_inv = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, 1>;
     k.threads = C::THREADS;
     k.transforms_per_cta = C::G;
     k.smem = C::SMEM;
@@ -127,12 +131,17 @@ bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs) {
 cudaError_t rows_prepare(RowsKernelInfo &k) {
     cudaError_t e = cudaSuccess;
     if (k.smem > 48 * 1024) {
-        e = cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k.fn_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
-        if (e != cudaSuccess) return e;
+        for (const void *fn : {k.fn, k.fn_persistent, k.fn_inv, k.fn_persistent_inv}) {
+            e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+            if (e != cudaSuccess) return e;
+        }
     }
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k.persist_ctas_per_sm, k.fn_persistent, k.threads, k.smem);
+    int inv_ctas = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k.persist_ctas_per_sm, k.fn_persistent, k.threads, k.smem);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&inv_ctas, k.fn_persistent_inv, k.threads, k.smem);
+    k.persist_ctas_per_sm = std::min(k.persist_ctas_per_sm, inv_ctas);
+    return e;
 }
 
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
@@ -140,13 +149,13 @@ cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, 
                         LoadOps ops) {
     if (batch == 0) return cudaSuccess;
     uint64_t ctas = (batch + k.transforms_per_cta - 1) / k.transforms_per_cta;
-    const void *fn = k.fn;
+    const bool inv = direction == GBFFT_INVERSE;
+    const void *fn = inv ? k.fn_inv : k.fn;
     if (persistent && k.persist_ctas_per_sm > 0 && sms > 0) {
-        fn = k.fn_persistent;
+        fn = inv ? k.fn_persistent_inv : k.fn_persistent;
         ctas = std::min<uint64_t>(ctas, (uint64_t)k.persist_ctas_per_sm * (uint64_t)sms);
     }
     if (ctas > 0x7fffffffull) return cudaErrorInvalidConfiguration;
-    const bool inv = direction == GBFFT_INVERSE;
     const float scale = inv ? ldexpf(1.0f, -logn) : 1.0f;
     float in_im = inv ? -1.0f : 1.0f;
     float out_re = scale, out_im = inv ? -scale : 1.0f;

@@ -58,7 +58,10 @@ struct RowRef {
 
 // G transforms of length 2^LOGN; thread tid = g*T + t.  `ref(g)` gives the
 // transform's RowRef.  smem holds G*N complex values (unused if NSUB == 1).
-template <int LOGN, int G, class RefFn, class Eng = DftRegs>
+// DIRC: direction known at compile time (-1 forward: no sign or scale work at
+// all; +1 inverse: conjugate on load, RowRef's scales on store), or 0 (taken
+// from RowRef per transform, for launches that mix directions).
+template <int LOGN, int G, int DIRC = 0, class RefFn, class Eng = DftRegs>
 __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem, const LoadOps &ops,
                                           Eng eng = Eng()) {
     using C = SubCfg<LOGN>;
@@ -78,8 +81,13 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
             v[e] = make_float2(v[e].x + z.x, v[e].y + z.y);
         }
     }
+    if constexpr (DIRC == 0) {
 #pragma unroll
-    for (int e = 0; e < C::E; ++e) v[e].y *= r.in_im;
+        for (int e = 0; e < C::E; ++e) v[e].y *= r.in_im;
+    } else if constexpr (DIRC > 0) {
+#pragma unroll
+        for (int e = 0; e < C::E; ++e) v[e].y = -v[e].y;
+    }
     if (ops.win != nullptr) {
 #pragma unroll
         for (int e = 0; e < C::E; ++e) {
@@ -98,7 +106,8 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
 #pragma unroll
             for (int q = 0; q < (1 << LR); ++q) {
                 const float2 y = v[b + q * NB];
-                st_stream(r.dst + subpass_out_pos<LR, LP, C::LOGT>(t, b, q), make_float2(y.x * r.out_re, y.y * r.out_im));
+                st_stream(r.dst + subpass_out_pos<LR, LP, C::LOGT>(t, b, q),
+                          DIRC < 0 ? y : make_float2(y.x * r.out_re, y.y * r.out_im));
             }
     }
 }

@@ -34,8 +34,10 @@ constexpr int kWindowMaxLogN = 24;
 
 // ---- single-pass kernel (fft_rows.cu) ------------------------------------
 struct RowsKernelInfo {
-    const void *fn = nullptr;
-    const void *fn_persistent = nullptr;  // tile loop with L2 prefetch of the next tile
+    const void *fn = nullptr;             // forward
+    const void *fn_persistent = nullptr;  // forward, tile loop with L2 prefetch of the next tile
+    const void *fn_inv = nullptr;         // the same two for the inverse
+    const void *fn_persistent_inv = nullptr;
     int persist_ctas_per_sm = 0;          // resident CTAs of fn_persistent (set by rows_prepare)
     int threads = 0;
     int transforms_per_cta = 0;

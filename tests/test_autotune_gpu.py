@@ -15,10 +15,14 @@ pytestmark = pytest.mark.gpu
 TOL_REL_L2 = 2e-6
 
 
-def _cache_line(logn, batch, direction, max_logr, persistent, precision=0, tile=0):
-    return json.dumps({"arch": "sm_103", "logn": logn, "precision": precision, "direction": direction,
-                       "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": persistent,
-                       "fused": 0, "tile": tile, "seconds": 1.0})
+def _cache_line(logn, batch, direction, max_logr, persistent, precision=0, tile=0, loge=None):
+    d = {"arch": "sm_103", "logn": logn, "precision": precision, "direction": direction,
+         "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": persistent,
+         "fused": 0, "tile": tile}
+    if loge is not None:  # lines without the key (older caches) mean 16 samples a thread
+        d["loge"] = loge
+    d["seconds"] = 1.0
+    return json.dumps(d)
 
 
 @pytest.mark.parametrize("logn,batch,max_logr,persistent", [
@@ -87,3 +91,56 @@ def test_forced_transforms_per_cta(tmp_path, monkeypatch, oracle, lib_built, log
         for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
             y = ctx.c2c_host(x, d)
             assert oracle.rel_l2(y, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2
+
+
+@pytest.mark.parametrize("logn", [13, 14])
+@pytest.mark.parametrize("persistent", [0, 1])
+@pytest.mark.parametrize("batch", [1, 37, 333])
+def test_forced_32_samples_per_thread(tmp_path, monkeypatch, oracle, lib_built, logn, persistent, batch):
+    """Single-pass N = 2^13 / 2^14 with 32 samples a thread (radix-32
+    sub-passes 32 x 32 x 8 and 32 x 32 x 16: two shared-memory exchanges
+    instead of three): FP64 gate, the reference path's 1e-3 gate, roundtrip;
+    batches below, near and above the persistent grid."""
+    import gbfft
+    from gbfft import signals
+    cache = tmp_path / "tune.jsonl"
+    cache.write_text("\n".join(_cache_line(logn, batch, d, 10, persistent, loge=5)
+                               for d in (gbfft.FORWARD, gbfft.INVERSE)) + "\n")
+    monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+    x = signals.normal_c64(batch, 1 << logn, seed=900 + logn + batch)
+    with gbfft.Context(0) as ctx:
+        y = ctx.c2c_host(x, gbfft.FORWARD)
+        assert oracle.rel_l2(y, oracle.fft64(x)) <= TOL_REL_L2
+        k = min(batch, 4)  # the reference path (a CPU restatement) on a few rows
+        assert oracle.max_abs_err(y[:k], oracle.ref_fft(x[:k])) <= 1e-3
+        z = ctx.c2c_host(y, gbfft.INVERSE)
+        assert oracle.rel_l2(z, oracle.fft64(y, inverse=True)) <= TOL_REL_L2
+        assert oracle.rel_l2(z, x) <= 1e-6
+
+
+@pytest.mark.parametrize("logn", [13, 14])
+def test_32_samples_per_thread_matches_16_with_load_ops(tmp_path, monkeypatch, oracle, lib_built, logn):
+    """The window and the pipeline noise applied on load give the same
+    transform in both thread layouts (to FP32 rounding)."""
+    import gbfft
+    from gbfft import signals
+    batch = 6
+    x = signals.uniform_c64(batch, 1 << logn, seed=950 + logn)
+    outs = []
+    for loge in (4, 5):
+        cache = tmp_path / f"tune_{loge}.jsonl"
+        cache.write_text("\n".join(_cache_line(logn, batch, d, 10, 0, loge=loge)
+                                   for d in (gbfft.FORWARD, gbfft.INVERSE)) + "\n")
+        monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+        with gbfft.Context(0) as ctx:
+            ctx.set_window(gbfft.WINDOW_HANN)
+            ctx.set_noise(7, 0.1)
+            outs.append([ctx.c2c_host(x, d) for d in (gbfft.FORWARD, gbfft.INVERSE)])
+    for a, b in zip(*outs):
+        assert oracle.rel_l2(b, a) <= 1e-6
+    # the window alone against FP64 of the windowed input
+    with gbfft.Context(0) as ctx:
+        ctx.set_window(gbfft.WINDOW_HANN)
+        w = signals.hann_window(1 << logn)
+        y = ctx.c2c_host(x, gbfft.FORWARD)
+        assert oracle.rel_l2(y, oracle.fft64(x * w[None, :])) <= TOL_REL_L2

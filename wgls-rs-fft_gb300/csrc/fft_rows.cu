@@ -25,32 +25,36 @@ namespace gbfft {
 
 // LOGS: log2 of the samples one CTA moves (2^12 by default; 2^11 and 2^13 are
 // the autotuner's "transforms per CTA" alternatives for N <= 2^11).
-template <int LOGN, int LOGS = 12>
-struct RowsCfg : SubCfg<LOGN> {
-    using S = SubCfg<LOGN>;
+// LE: log2 of the samples a thread holds: 4, or 5 for N = 2^13 / 2^14, whose
+// radix-32 sub-passes (32 x 32 x 8, 32 x 32 x 16) need two exchanges instead
+// of three (16 x 16 x 16 x 2, 16 x 16 x 16 x 4) at 128 registers a thread.
+template <int LOGN, int LOGS = 12, int LE = 4>
+struct RowsCfg : SubCfg<LOGN, LE> {
+    using S = SubCfg<LOGN, LE>;
     static constexpr int TILE = 1 << LOGS;
     static constexpr int G_BY_SAMPLES = S::N >= TILE ? 1 : TILE / S::N;
     static constexpr int G_BY_THREADS = S::T >= TILE / 16 ? 1 : (TILE / 16) / S::T;
     static constexpr int G = G_BY_SAMPLES < G_BY_THREADS ? G_BY_SAMPLES : G_BY_THREADS;
     static constexpr int THREADS = G * S::T;
-    static constexpr int MINB = THREADS >= 1024 ? 1 : 1024 / THREADS;  // 64 registers a thread
+    static constexpr int REGS = LE == 4 ? 64 : 128;  // registers a thread
+    static constexpr int MINB = THREADS * REGS >= 65536 ? 1 : 65536 / (THREADS * REGS);
     static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * S::N * sizeof(float2) : 0;
 };
 
 // DIRC: -1 forward, +1 inverse (a launch has one direction, so the sign and
 // scale work is resolved at compile time).
-template <int LOGN, int LOGS, int DIRC>
-__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS>::THREADS, RowsCfg<LOGN, LOGS>::MINB)
+template <int LOGN, int LOGS, int DIRC, int LE>
+__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS, LE>::THREADS, RowsCfg<LOGN, LOGS, LE>::MINB)
 fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                 float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
-    using C = RowsCfg<LOGN, LOGS>;
+    using C = RowsCfg<LOGN, LOGS, LE>;
     extern __shared__ float2 smem_rows[];
     auto ref = [&](int g) {
         const uint64_t row = (uint64_t)blockIdx.x * C::G + g;
         return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
                       (uint32_t)row};
     };
-    rows_tile<LOGN, C::G, DIRC>(ref, tw, smem_rows, ops);
+    rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops);
 }
 
 // Persistent variant for the sizes whose per-transform footprint allows only
@@ -58,11 +62,11 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
 // blockIdx.x, +gridDim.x, ... and, before computing a tile, asks L2 for the
 // next one (one 128-byte line per thread), so the HBM fetch of tile i+1
 // overlaps the shared-memory sub-passes of tile i.
-template <int LOGN, int LOGS, int DIRC>
-__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS>::THREADS, RowsCfg<LOGN, LOGS>::MINB)
+template <int LOGN, int LOGS, int DIRC, int LE>
+__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS, LE>::THREADS, RowsCfg<LOGN, LOGS, LE>::MINB)
 fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
                            float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
-    using C = RowsCfg<LOGN, LOGS>;
+    using C = RowsCfg<LOGN, LOGS, LE>;
     extern __shared__ float2 smem_rows[];
     constexpr uint32_t kTileSamples = C::G * C::N;
     constexpr uint32_t kLines = kTileSamples * sizeof(float2) / 128;
@@ -79,7 +83,7 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
             return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
                       (uint32_t)row};
         };
-        rows_tile<LOGN, C::G, DIRC>(ref, tw, smem_rows, ops);
+        rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops);
         __syncthreads();  // shared memory is reused by the next tile
     }
 }
@@ -88,21 +92,30 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
 // host side
 // ---------------------------------------------------------------------------
 
-template <int LOGN, int LOGS = 12>
+template <int LOGN, int LOGS = 12, int LE = 4>
 static void rows_describe(RowsKernelInfo &k) {
-    using C = RowsCfg<LOGN, LOGS>;
-    k.fn = (const void *)fft_rows_kernel<LOGN, LOGS, -1>;
-    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, -1>;
-    k.fn_inv = (const void *)fft_rows_kernel<LOGN, LOGS, 1>;
-    k.fn_persistent_inv = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, 1>;
+    using C = RowsCfg<LOGN, LOGS, LE>;
+    k.fn = (const void *)fft_rows_kernel<LOGN, LOGS, -1, LE>;
+    k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, -1, LE>;
+    k.fn_inv = (const void *)fft_rows_kernel<LOGN, LOGS, 1, LE>;
+    k.fn_persistent_inv = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, 1, LE>;
     k.threads = C::THREADS;
     k.transforms_per_cta = C::G;
     k.smem = C::SMEM;
-    k.nseg = subcfg_segments<LOGN>(k.segs, 0);
+    k.nseg = subcfg_segments<LOGN, LE>(k.segs, 0);
     k.tw_entries = C::tw_entries();
 }
 
-bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs) {
+bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs, int loge) {
+    if (loge == 5) {  // 32 samples a thread: N = 2^13, 2^14 (one transform a CTA)
+        if (logs != 12) return false;
+        switch (logn) {
+            case 13: rows_describe<13, 12, 5>(k); return true;
+            case 14: rows_describe<14, 12, 5>(k); return true;
+            default: return false;
+        }
+    }
+    if (loge != 4) return false;
     if (logs == 11 || logs == 13) {  // other tile sizes for the sizes that batch transforms in a CTA
         switch (logn) {
 #define GBFFT_ROWS_TILE(L)                                              \

@@ -19,9 +19,11 @@
 
 namespace gbfft {
 
-template <int LOGN>
+// LE: log2 of the samples a thread holds (4, or 5 for the 32-sample tiles
+// of N = 2^13 / 2^14, which need one exchange fewer).
+template <int LOGN, int LE = 4>
 struct SubCfg {
-    static constexpr int LOGE = LOGN < 4 ? LOGN : 4;
+    static constexpr int LOGE = LOGN < LE ? LOGN : LE;
     static constexpr int N = 1 << LOGN;
     static constexpr int E = 1 << LOGE;
     static constexpr int LOGT = LOGN - LOGE;
@@ -71,10 +73,51 @@ __device__ __forceinline__ float2 mul_w16c(float2 a) {
     }
 }
 
+// a * W_32^I for a compile-time I: even I through mul_w16c, odd I with the
+// constants cos(pi k / 16), sin(pi k / 16) (k = 1, 3; k = 5, 7 swap them).
+constexpr float kCos1_32 = 0.98078528040323044913f;  // cos(pi/16)
+constexpr float kSin1_32 = 0.19509032201612826785f;  // sin(pi/16)
+constexpr float kCos3_32 = 0.83146961230254523708f;  // cos(3 pi/16)
+constexpr float kSin3_32 = 0.55557023301960222474f;  // sin(3 pi/16)
+template <int I>
+__device__ __forceinline__ float2 mul_w32c(float2 a) {
+    constexpr int i = I & 31;
+    if constexpr ((i & 1) == 0) return mul_w16c<i / 2>(a);
+    else if constexpr (i > 8) return mul_mi(mul_w32c<i - 8>(a));  // W_32^8 = -i
+    else {
+        // a * (c - i s) with (c, s) = (cos, sin)(pi i / 16)
+        constexpr float c = i == 1 ? kCos1_32 : (i == 3 ? kCos3_32 : (i == 5 ? kSin3_32 : kSin1_32));
+        constexpr float sn = i == 1 ? kSin1_32 : (i == 3 ? kSin3_32 : (i == 5 ? kCos3_32 : kCos1_32));
+        return make_float2(fmaf(a.x, c, a.y * sn), fmaf(a.y, c, -a.x * sn));
+    }
+}
+
+// 32-point DFT: radix-2 decimation in frequency, then two 16-point DFTs.
+template <> struct Dft<32> {
+    __device__ __forceinline__ static void run(float2 *x) {
+        float2 a[16], b[16];
+        auto split = [&](auto kc) {
+            constexpr int k = decltype(kc)::value;
+            a[k] = cadd(x[k], x[k + 16]);
+            b[k] = mul_w32c<k>(csub(x[k], x[k + 16]));
+        };
+        [&]<int... Ks>(std::integer_sequence<int, Ks...>) {
+            (split(std::integral_constant<int, Ks>{}), ...);
+        }(std::make_integer_sequence<int, 16>{});
+        Dft<16>::run(a);
+        Dft<16>::run(b);
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            x[2 * k] = a[k];
+            x[2 * k + 1] = b[k];
+        }
+    }
+};
+
 template <int LOGE, int LOGR, int B, int M>
 struct FactoredTw {
-    // W_E^{m b} with E = 2^LOGE expressed in sixteenths of a turn
-    static constexpr int idx16 = ((M * B) << (4 - LOGE)) & 15;
+    // W_E^{m b} with E = 2^LOGE expressed in 32nds of a turn
+    static constexpr int idx32 = ((M * B) << (5 - LOGE)) & 31;
 };
 
 // Engine of the radix-R butterflies: FP32 in registers (DftRegs) or, for the
@@ -99,7 +142,7 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
             for (int m = 0; m < R; ++m) x[m] = v[b + m * NB];
             auto apply = [&](auto mc) {
                 constexpr int M = decltype(mc)::value;
-                if constexpr (M > 0) x[M] = cmul(mul_w16c<FactoredTw<LOGE, LOGR, b, M>::idx16>(x[M]), wt[M]);
+                if constexpr (M > 0) x[M] = cmul(mul_w32c<FactoredTw<LOGE, LOGR, b, M>::idx32>(x[M]), wt[M]);
             };
             [&]<int... Ms>(std::integer_sequence<int, Ms...>) {
                 (apply(std::integral_constant<int, Ms>{}), ...);
@@ -131,19 +174,19 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
 }
 
 // Twiddle-table segments of sub-passes 1..NSUB-1 (offsets from `base`).
-template <int LOGN>
+template <int LOGN, int LE = 4>
 inline int subcfg_segments(TwiddleSegment *out, uint64_t base) {
-    using C = SubCfg<LOGN>;
+    using C = SubCfg<LOGN, LE>;
     for (int i = 1; i < C::NSUB; ++i)
         out[i - 1] = TwiddleSegment{base + (uint64_t)C::tw_offset(i), (uint64_t)C::tw_count(i), 0, C::tw_logm(i),
                                     C::tw_logp(i), 0};
     return C::NSUB - 1;
 }
 
-// Sub-pass I of the schedule of SubCfg<LOGN> (twiddle table already offset).
-template <int LOGN, int I, class Eng = DftRegs>
-__device__ __forceinline__ void subpass_run(float2 (&v)[SubCfg<LOGN>::E], int t, const float2 *tw_all, Eng &eng) {
-    using C = SubCfg<LOGN>;
+// Sub-pass I of the schedule of SubCfg<LOGN, LE> (twiddle table already offset).
+template <int LOGN, int I, int LE = 4, class Eng = DftRegs>
+__device__ __forceinline__ void subpass_run(float2 (&v)[SubCfg<LOGN, LE>::E], int t, const float2 *tw_all, Eng &eng) {
+    using C = SubCfg<LOGN, LE>;
     subpass_compute<C::LOGE, C::logr(I), C::logp(I), C::LOGT, C::factored(I), Eng>(v, t, tw_all + C::tw_offset(I),
                                                                                      eng);
 }

@@ -15,15 +15,19 @@ namespace gbfft {
 constexpr int kColsLog = 4;
 constexpr int kCols = 1 << kColsLog;
 
+// Exchange-buffer position of element a after a sub-pass with p = 2^logp: for
+// p < 2^LE the low LE bits are XORed with (a >> LE) << logp (a bijection), which
+// spreads the stride-p writes over the banks.
+template <int LE = 4>
 __device__ __forceinline__ int swz(int a, int logp) {
-    return logp < 4 ? (a ^ (((a >> 4) << logp) & 15)) : a;
+    return logp < LE ? (a ^ (((a >> LE) << logp) & ((1 << LE) - 1))) : a;
 }
 
 // Sub-passes 1..NSUB-1 of a row transform held as v[] by thread t, exchanged
 // through buf (XOR-swizzled positions).
-template <int LOGN, int I, bool DONE = (I >= SubCfg<LOGN>::NSUB)>
+template <int LOGN, int I, int LE = 4, bool DONE = (I >= SubCfg<LOGN, LE>::NSUB)>
 struct RowsChain {
-    using C = SubCfg<LOGN>;
+    using C = SubCfg<LOGN, LE>;
     template <class Eng>
     __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, float2 *buf, const float2 *tw, Eng &eng) {
         constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);  // previous sub-pass
@@ -32,18 +36,19 @@ struct RowsChain {
         for (int b = 0; b < (C::E >> PR); ++b)
 #pragma unroll
             for (int q = 0; q < (1 << PR); ++q)
-                buf[swz(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP)] = v[b + q * (C::E >> PR)];
+                buf[swz<C::LOGE>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP)] = v[b + q * (C::E >> PR)];
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < C::E; ++e) v[e] = buf[swz(t + C::T * e, PP)];
-        subpass_run<LOGN, I>(v, t, tw, eng);
-        RowsChain<LOGN, I + 1>::run(v, t, buf, tw, eng);
+        for (int e = 0; e < C::E; ++e) v[e] = buf[swz<C::LOGE>(t + C::T * e, PP)];
+        subpass_run<LOGN, I, LE>(v, t, tw, eng);
+        RowsChain<LOGN, I + 1, LE>::run(v, t, buf, tw, eng);
     }
 };
-template <int LOGN, int I>
-struct RowsChain<LOGN, I, true> {
+template <int LOGN, int I, int LE>
+struct RowsChain<LOGN, I, LE, true> {
     template <class Eng>
-    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGN>::E], int, float2 *, const float2 *, Eng &) {}
+    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGN, LE>::E], int, float2 *, const float2 *,
+                                               Eng &) {}
 };
 
 // Per-transform access for rows_tile: where transform g of the tile lives,
@@ -61,10 +66,11 @@ struct RowRef {
 // DIRC: direction known at compile time (-1 forward: no sign or scale work at
 // all; +1 inverse: conjugate on load, RowRef's scales on store), or 0 (taken
 // from RowRef per transform, for launches that mix directions).
-template <int LOGN, int G, int DIRC = 0, class RefFn, class Eng = DftRegs>
+// LE: log2 of the samples a thread holds (SubCfg).
+template <int LOGN, int G, int DIRC = 0, int LE = 4, class RefFn, class Eng = DftRegs>
 __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ tw, float2 *smem, const LoadOps &ops,
                                           Eng eng = Eng()) {
-    using C = SubCfg<LOGN>;
+    using C = SubCfg<LOGN, LE>;
     const int tid = threadIdx.x;
     const int g = tid >> C::LOGT;
     const int t = tid & (C::T - 1);
@@ -95,8 +101,8 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
             v[e] = make_float2(v[e].x * w, v[e].y * w);
         }
     }
-    subpass_run<LOGN, 0>(v, t, tw, eng);
-    RowsChain<LOGN, 1>::run(v, t, smem + g * C::N, tw, eng);
+    subpass_run<LOGN, 0, LE>(v, t, tw, eng);
+    RowsChain<LOGN, 1, LE>::run(v, t, smem + g * C::N, tw, eng);
     // last sub-pass (p R = N): output q of butterfly j sits at j + q p
     if (r.active) {
         constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);

@@ -46,8 +46,9 @@ struct RowsKernelInfo {
     int nseg = 0;
     int tw_entries = 0;
 };
-// logs: log2 of the samples a CTA moves (12; 11 or 13 for N = 2^6 .. 2^11)
-bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs = 12);
+// logs: log2 of the samples a CTA moves (12; 11 or 13 for N = 2^6 .. 2^11);
+// loge: log2 of the samples a thread holds (4; 5 for N = 2^13, 2^14)
+bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs = 12, int loge = 4);
 cudaError_t rows_prepare(RowsKernelInfo &k);
 // persistent: use fn_persistent with at most persist_ctas_per_sm * sms CTAs.
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,

@@ -82,10 +82,19 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         // other CTA to overlap with at 2^14, so prefetch helps there
         RowsKernelInfo ri;
         if (rows_kernel_info(logn, ri, 11)) c.push_back(PlanVariant{10, false, false, 11});
+        // 32 samples a thread (radix-32 sub-passes, one exchange fewer): measured
+        // fastest at 2^13 (330 vs 303 GSa/s); at 2^14 its 16 warps per SM lose to
+        // the 32 of the 16-sample layout (253-262 vs 271), so there it is only a candidate
+        const bool e32 = rows_kernel_info(logn, ri, 12, 5);
+        if (e32 && logn == 13) c.push_back(PlanVariant{10, false, false, 0, 5});
         const bool big = logn >= 14;
         c.push_back(PlanVariant{10, big});
         c.push_back(PlanVariant{10, !big});
         if (rows_kernel_info(logn, ri, 13)) c.push_back(PlanVariant{10, false, false, 13});
+        if (e32) {
+            if (logn != 13) c.push_back(PlanVariant{10, false, false, 0, 5});
+            c.push_back(PlanVariant{10, true, false, 0, 5});
+        }
         FusedDesc fd;
         if (precision == GBFFT_PREC_FP32 && fused2_kernel_info(7, logn - 7, fd)) c.push_back(PlanVariant{10, false, true});
         return c;
@@ -126,7 +135,7 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
     // tiles (a tuner candidate)
     const bool small_fused = v.fused && !tc && (logn == 13 || logn == 14);
     if (logn <= kRowsMaxLogN && !small_fused) {
-        if (!rows_kernel_info(logn, p.rows, v.tile ? v.tile : 12)) {
+        if (!rows_kernel_info(logn, p.rows, v.tile ? v.tile : 12, v.loge)) {
             why = "no single-pass kernel";
             return GBFFT_ERR_UNSUPPORTED;
         }

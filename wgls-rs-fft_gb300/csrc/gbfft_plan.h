@@ -65,14 +65,17 @@ struct PlanVariant {
     bool persistent = false;
     bool fused = false;
     int tile = 0;  // single pass: log2 of the samples a CTA moves (0: 2^12), i.e. transforms per CTA
+    int loge = 4;  // single pass: log2 of the samples a thread holds (5: radix-32 sub-passes, N = 2^13, 2^14)
     bool operator<(const PlanVariant &o) const {
         if (max_logr != o.max_logr) return max_logr < o.max_logr;
         if (persistent != o.persistent) return persistent < o.persistent;
         if (fused != o.fused) return fused < o.fused;
-        return tile < o.tile;
+        if (tile != o.tile) return tile < o.tile;
+        return loge < o.loge;
     }
     bool operator==(const PlanVariant &o) const {
-        return max_logr == o.max_logr && persistent == o.persistent && fused == o.fused && tile == o.tile;
+        return max_logr == o.max_logr && persistent == o.persistent && fused == o.fused && tile == o.tile &&
+               loge == o.loge;
     }
 };
 

@@ -26,22 +26,22 @@ def torch():
     return t
 
 
-def _force(tmp_path, monkeypatch, logn, batch, fused, max_logr=10):
+def _force(tmp_path, monkeypatch, logn, batch, fused, max_logr=10, loge=4):
     import gbfft
     lines = []
     for d in (gbfft.FORWARD, gbfft.INVERSE):
         lines.append(json.dumps({"arch": "sm_103", "logn": logn, "precision": 0, "direction": d,
                                  "batch_log2": batch.bit_length() - 1, "max_logr": max_logr, "persistent": 0,
-                                 "fused": int(fused), "tile": 0, "seconds": 1.0}))
-    cache = tmp_path / f"tune_{int(fused)}.jsonl"
+                                 "fused": int(fused), "tile": 0, "loge": loge, "seconds": 1.0}))
+    cache = tmp_path / f"tune_{int(fused)}_{loge}.jsonl"
     cache.write_text("\n".join(lines) + "\n")
     monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
 
 
-def _run(torch, x, direction, fused, tmp_path, monkeypatch, repeats=1, noise=None):
+def _run(torch, x, direction, fused, tmp_path, monkeypatch, repeats=1, noise=None, loge=4):
     import gbfft
     batch, n = x.shape
-    _force(tmp_path, monkeypatch, n.bit_length() - 1, batch, fused)
+    _force(tmp_path, monkeypatch, n.bit_length() - 1, batch, fused, loge=loge)
     dx = torch.from_numpy(x).cuda()
     outs = []
     with gbfft.Context(0) as ctx:
@@ -193,3 +193,25 @@ def test_fused_radix128_pair_for_single_pass_sizes(torch, oracle, lib_built, tmp
         (yf,), lf = _run(torch, x, d, True, tmp_path, monkeypatch)
         assert lf == 1
         assert oracle.rel_l2(yf, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2
+
+
+@pytest.mark.parametrize("logn,batch", [(17, 1), (17, 33), (18, 5), (18, 40), (19, 3), (20, 2), (20, 9)])
+def test_fused_32_samples_per_thread(torch, oracle, lib_built, tmp_path, monkeypatch, logn, batch):
+    """The pass pair with 32 samples a thread (radix-32 sub-passes: a
+    radix-2^9 pass as 32 x 16 instead of 16 x 16 x 2, 2^10 as 32 x 32 instead
+    of 16 x 16 x 4), with its own sub-pass tables: FP64 gate, agreement with
+    the 16-sample pair to FP32 rounding, repeated launches, noise on load."""
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=340 + logn + batch)
+    for d, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        (y5, y5b), l5 = _run(torch, x, d, True, tmp_path, monkeypatch, repeats=2, loge=5)
+        (y4,), _ = _run(torch, x, d, True, tmp_path, monkeypatch, loge=4)
+        assert l5 == 2  # one launch a transform
+        assert np.array_equal(y5, y5b)
+        assert oracle.rel_l2(y5, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2
+        assert oracle.rel_l2(y5, y4) <= 1e-6
+    z = np.zeros((3, 1 << logn), np.complex64)
+    (n5,), _ = _run(torch, z, gbfft.FORWARD, True, tmp_path, monkeypatch, noise=(11, 0.5), loge=5)
+    (n4,), _ = _run(torch, z, gbfft.FORWARD, True, tmp_path, monkeypatch, noise=(11, 0.5), loge=4)
+    assert np.abs(n4).max() > 0 and oracle.rel_l2(n5, n4) <= 1e-6

@@ -39,12 +39,14 @@ namespace gbfft {
 
 // LOGPA: log2 of the product of the radices before pass A (0: A is the first
 // pass).  Both passes use every thread; for LOGPA > 0 both radices are equal.
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA>
+// LE: log2 of the samples a thread holds (4: 64 registers a thread; 5: radix-32
+// sub-passes, 128 registers a thread).
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, int LE = 4>
 struct FusedCfg {
-    static constexpr int NGA = THREADS >> LOGRA;
-    static constexpr int NGB = THREADS >> LOGRB;
+    static constexpr int NGA = (THREADS << (LE - 4)) >> LOGRA;
+    static constexpr int NGB = (THREADS << (LE - 4)) >> LOGRB;
     static_assert(NGA >= 1 && NGB >= 1, "CTA narrower than a radix");
-    static_assert(PassTileCfg<LOGRA, NGA>::THREADS == THREADS && PassTileCfg<LOGRB, NGB>::THREADS == THREADS,
+    static_assert(PassTileCfg<LOGRA, NGA, LE>::THREADS == THREADS && PassTileCfg<LOGRB, NGB, LE>::THREADS == THREADS,
                   "both passes must use every thread");
     static_assert(LOGPA == 0 ? LOGN == LOGRA + LOGRB : (LOGRA == LOGRB && NGA == 1 && LOGPA >= 4),
                   "two-pass transform, or the last two passes (R1, R, R) of three with one column group a tile");
@@ -52,11 +54,12 @@ struct FusedCfg {
     static constexpr int LOGPB = LOGPA + LOGRA;
     // groups per transform and tiles of each pass per group
     static constexpr uint32_t GPT = FIRST_A ? 1u : (1u << LOGPA) / kCols;
-    static constexpr uint32_t T = FIRST_A ? (1u << LOGN) / (16u * THREADS) : (1u << LOGRB);
-    static constexpr uint64_t GROUP_SAMPLES = (uint64_t)T * 16u * THREADS;
-    static constexpr size_t EA = PassTileCfg<LOGRA, NGA>::SMEM_ELEMS, EB = PassTileCfg<LOGRB, NGB>::SMEM_ELEMS;
+    static constexpr uint32_t T = FIRST_A ? (1u << LOGN) / ((1u << LE) * THREADS) : (1u << LOGRB);
+    static constexpr uint64_t GROUP_SAMPLES = (uint64_t)T * (1u << LE) * THREADS;
+    static constexpr size_t EA = PassTileCfg<LOGRA, NGA, LE>::SMEM_ELEMS, EB = PassTileCfg<LOGRB, NGB, LE>::SMEM_ELEMS;
     static constexpr size_t SMEM = (EA > EB ? EA : EB) * sizeof(float2);
-    static constexpr int MINB = THREADS >= 1024 ? 1 : 1024 / THREADS;
+    static constexpr int REGS = LE == 4 ? 64 : 128;
+    static constexpr int MINB = THREADS * REGS >= 65536 ? 1 : 65536 / (THREADS * REGS);
 };
 
 struct FusedParams {
@@ -118,9 +121,9 @@ __device__ __forceinline__ uint32_t fused_claim(const FusedParams &P) {
 // after an error) is exhausted.  `Eng` runs the radix-16 butterflies (FP32
 // registers, or the tensor cores for the split forms); every thread of the
 // CTA takes part in every item.
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, class Eng>
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, int LE = 4, class Eng>
 __device__ __forceinline__ void fused_loop(const FusedParams &P, float2 *smem_f, Eng eng) {
-    using C = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA>;
+    using C = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>;
     constexpr uint32_t T = C::T, GPT = C::GPT;
     // Claimed queue positions, double-buffered: slot `par` holds the current
     // item, slot par ^ 1 receives the next claim while the tile runs.
@@ -160,7 +163,7 @@ __device__ __forceinline__ void fused_loop(const FusedParams &P, float2 *smem_f,
             a.coherent_load = false;
             a.keep_l2 = true;
             a.ops = C::FIRST_A ? P.ops : LoadOps{nullptr, 0u, 0.f, 0u};
-            pass_tile<LOGRA, C::NGA, C::FIRST_A, Eng, LOGN, LOGPA>(a, smem_f, eng);
+            pass_tile<LOGRA, C::NGA, C::FIRST_A, Eng, LOGN, LOGPA, LE>(a, smem_f, eng);
         } else {
             if (threadIdx.x == 0) {
                 uint32_t polls = 0;
@@ -187,7 +190,7 @@ __device__ __forceinline__ void fused_loop(const FusedParams &P, float2 *smem_f,
             a.out_im = P.out_im;
             a.coherent_load = true;
             a.ops = LoadOps{nullptr, 0u, 0.f, 0u};
-            pass_tile<LOGRB, C::NGB, false, Eng, LOGN, C::LOGPB>(a, smem_f, eng);
+            pass_tile<LOGRB, C::NGB, false, Eng, LOGN, C::LOGPB, LE>(a, smem_f, eng);
         }
         __syncthreads();  // the tile's stores are issued; shared memory is free
         if (threadIdx.x == 0) {
@@ -218,18 +221,19 @@ __device__ __forceinline__ void fused_finish(const FusedParams &P) {
     }
 }
 
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA>
-__global__ void __launch_bounds__(THREADS, (FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA>::MINB))
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, int LE = 4>
+__global__ void __launch_bounds__(THREADS, (FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>::MINB))
 fft_fused_kernel(FusedParams P) {
     extern __shared__ float2 smem_f[];
-    fused_loop<LOGRA, LOGRB, THREADS, LOGN, LOGPA>(P, smem_f, DftRegs());
+    fused_loop<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>(P, smem_f, DftRegs());
     fused_finish<THREADS>(P);
 }
 
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA>
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, int LE = 4>
 inline void fused_describe(FusedDesc &d) {
-    using C = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA>;
-    d.fn = (const void *)fft_fused_kernel<LOGRA, LOGRB, THREADS, LOGN, LOGPA>;
+    using C = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>;
+    d.fn = (const void *)fft_fused_kernel<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>;
+    d.loge = LE;
     d.threads = THREADS;
     d.smem = C::SMEM;
     d.logra = LOGRA;

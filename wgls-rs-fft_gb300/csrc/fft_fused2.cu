@@ -9,7 +9,18 @@
 
 namespace gbfft {
 
-bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d) {
+bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d, int loge) {
+    if (loge == 5) {
+#define GBFFT_F2E(A, B, T) \
+    if (logr1 == A && logr2 == B) { fused_describe<A, B, T, A + B, 0, 5>(d); return true; }
+        GBFFT_F2E(9, 8, 256)
+        GBFFT_F2E(9, 9, 256)
+        GBFFT_F2E(10, 9, 512)
+        GBFFT_F2E(10, 10, 512)
+#undef GBFFT_F2E
+        return false;
+    }
+    if (loge != 4) return false;
 #define GBFFT_F2(A, B, T) \
     if (logr1 == A && logr2 == B) { fused_describe<A, B, T, A + B, 0>(d); return true; }
     GBFFT_F2(7, 6, 128)
@@ -22,6 +33,17 @@ bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d) {
     GBFFT_F2(10, 10, 1024)
 #undef GBFFT_F2
     return false;
+}
+
+int pass_sub_segments(int logr, int loge, TwiddleSegment *out, uint64_t base, int &entries) {
+    switch (loge * 16 + logr) {
+#define GBFFT_SEG(E, R) \
+    case E * 16 + R: entries = SubCfg<R, E>::tw_entries(); return subcfg_segments<R, E>(out, base);
+        GBFFT_SEG(5, 8) GBFFT_SEG(5, 9) GBFFT_SEG(5, 10)
+        GBFFT_SEG(4, 5) GBFFT_SEG(4, 6) GBFFT_SEG(4, 7) GBFFT_SEG(4, 8) GBFFT_SEG(4, 9) GBFFT_SEG(4, 10)
+#undef GBFFT_SEG
+        default: entries = 0; return -1;
+    }
 }
 
 cudaError_t fused_prepare(FusedDesc &d) {

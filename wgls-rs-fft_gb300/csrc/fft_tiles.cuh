@@ -120,9 +120,9 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
 
 // ---- global-pass tiles -----------------------------------------------------
 
-template <int LOGR, int I, bool DONE = (I >= SubCfg<LOGR>::NSUB)>
+template <int LOGR, int I, int LE = 4, bool DONE = (I >= SubCfg<LOGR, LE>::NSUB)>
 struct PassChain {
-    using C = SubCfg<LOGR>;
+    using C = SubCfg<LOGR, LE>;
     template <class Eng>
     __device__ __forceinline__ static void run(float2 (&v)[C::E], int t, int c, float2 *buf, const float2 *tw,
                                                Eng &eng) {
@@ -136,14 +136,14 @@ struct PassChain {
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < C::E; ++e) v[e] = buf[((t + C::T * e) << kColsLog) + c];
-        subpass_run<LOGR, I>(v, t, tw, eng);
-        PassChain<LOGR, I + 1>::run(v, t, c, buf, tw, eng);
+        subpass_run<LOGR, I, LE>(v, t, tw, eng);
+        PassChain<LOGR, I + 1, LE>::run(v, t, c, buf, tw, eng);
     }
 };
-template <int LOGR, int I>
-struct PassChain<LOGR, I, true> {
+template <int LOGR, int I, int LE>
+struct PassChain<LOGR, I, LE, true> {
     template <class Eng>
-    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR>::E], int, int, float2 *, const float2 *,
+    __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR, LE>::E], int, int, float2 *, const float2 *,
                                                Eng &) {}
 };
 
@@ -152,9 +152,9 @@ __device__ __forceinline__ float2 twiddle_2level(const float2 *__restrict__ lo, 
     return cmul(ld_tw(hi + (ex >> split)), ld_tw(lo + (ex & ((1u << split) - 1))));
 }
 
-template <int LOGR, int NG>
+template <int LOGR, int NG, int LE = 4>
 struct PassTileCfg {
-    using S = SubCfg<LOGR>;
+    using S = SubCfg<LOGR, LE>;
     static constexpr int THREADS = NG * kCols * S::T;
     static constexpr int COLTW_STRIDE = S::E + 1;  // padded: conflict-free column reads
     static constexpr size_t SMEM_ELEMS = (size_t)NG * kCols * S::N + (size_t)NG * kCols * COLTW_STRIDE;
@@ -179,11 +179,12 @@ struct PassArgs {
 // NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
 // LOGN_CT / LOGP_CT: log2 N and log2 p when the caller knows them at compile
 // time (0 / -1: taken from a.logn / a.logp).  Constant sizes turn every
-// strided address and twiddle index into immediates.
-template <int LOGR, int NG, bool FIRST, class Eng = DftRegs, int LOGN_CT = 0, int LOGP_CT = -1>
+// strided address and twiddle index into immediates.  LE: log2 of the
+// samples a thread holds (SubCfg; the sub-pass tables in a.tw_sub follow it).
+template <int LOGR, int NG, bool FIRST, class Eng = DftRegs, int LOGN_CT = 0, int LOGP_CT = -1, int LE = 4>
 __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng eng = Eng()) {
-    using C = SubCfg<LOGR>;
-    using K = PassTileCfg<LOGR, NG>;
+    using C = SubCfg<LOGR, LE>;
+    using K = PassTileCfg<LOGR, NG, LE>;
     constexpr int R = C::N, T = C::T, E = C::E;
     const int tid = threadIdx.x;
     const int grp = tid / (kCols * T);
@@ -243,8 +244,8 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = cmul(v[e], cmul(w, coltw[c * K::COLTW_STRIDE + e]));
     }
-    subpass_run<LOGR, 0>(v, t, a.tw_sub, eng);
-    PassChain<LOGR, 1>::run(v, t, c, buf, a.tw_sub, eng);
+    subpass_run<LOGR, 0, LE>(v, t, a.tw_sub, eng);
+    PassChain<LOGR, 1, LE>::run(v, t, c, buf, a.tw_sub, eng);
 
     constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
     constexpr int NB = E >> LR;

@@ -109,6 +109,11 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         bool dup = false;
         for (const PlanVariant &v : c) dup |= split_passes(logn, v.max_logr) == parts;
         if (dup || parts[0] < 5) continue;
+        // the pair with 32 samples a thread (radix-32 sub-passes) first where it
+        // exists: measured faster at 2^17..2^20 (177 / 178.5 / 150.7 / 155.9
+        // against 174.7 / 166.2 / 145.6 / 144.7 GSa/s)
+        if (!tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd, 5))
+            c.push_back(PlanVariant{m, false, true, 0, 5});
         if (parts.size() == 2 && (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, fd)
                                      : fused2_kernel_info(parts[0], parts[1], fd)))
             c.push_back(PlanVariant{m, false, true});
@@ -174,7 +179,28 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
         if (fused3 || (v.fused && parts.size() == 2 &&
                        (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, p.fused)
-                           : fused2_kernel_info(parts[0], parts[1], p.fused)))) {
+                           : fused2_kernel_info(parts[0], parts[1], p.fused, v.loge)))) {
+            if (p.fused.loge != 4) {
+                // the pair's tiles follow their own sub-pass schedule: append its tables
+                int ea = 0, eb = 0;
+                TwiddleSegment ts[kMaxSub];
+                const int na = pass_sub_segments(parts[0], p.fused.loge, ts, p.tw_entries, ea);
+                if (na < 0) {
+                    why = "no sub-pass tables for the pair";
+                    return GBFFT_ERR_UNSUPPORTED;
+                }
+                segs.insert(segs.end(), ts, ts + na);
+                p.fused.sub_off_a = (int64_t)p.tw_entries;
+                p.tw_entries += (uint64_t)ea;
+                const int nb = pass_sub_segments(parts[1], p.fused.loge, ts, p.tw_entries, eb);
+                if (nb < 0) {
+                    why = "no sub-pass tables for the pair";
+                    return GBFFT_ERR_UNSUPPORTED;
+                }
+                segs.insert(segs.end(), ts, ts + nb);
+                p.fused.sub_off_b = (int64_t)p.tw_entries;
+                p.tw_entries += (uint64_t)eb;
+            }
             if ((e = fused_prepare(p.fused)) != cudaSuccess) {
                 why = cudaGetErrorString(e);
                 return GBFFT_ERR_CUDA;
@@ -248,8 +274,10 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
             ++launches;
             pair_in = (const float2 *)ws.ptr;
         }
-        e = fused_launch(p.fused, pair_in, out, batch, p.tw + p.passes[a].sub_tw_offset,
-                         p.tw + p.passes[a + 1].sub_tw_offset, p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset,
+        const float2 *tw_a = p.fused.sub_off_a >= 0 ? p.tw + p.fused.sub_off_a : p.tw + p.passes[a].sub_tw_offset;
+        const float2 *tw_b =
+            p.fused.sub_off_b >= 0 ? p.tw + p.fused.sub_off_b : p.tw + p.passes[a + 1].sub_tw_offset;
+        e = fused_launch(p.fused, pair_in, out, batch, tw_a, tw_b, p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset,
                          (inv && !pair3) ? -1.0f : 1.0f, scale, inv ? -scale : 1.0f,
                          pair3 ? LoadOps{nullptr, 0u, 0.f, 0u} : ops, (uint32_t *)ctr->ptr, err, p.sms, stream,
                          p.gtab);

@@ -52,6 +52,10 @@ struct FusedDesc {
     uint64_t group_samples = 0;
     int ctas_per_sm = 0;
     int tmem_cols = 0;  // split forms: TMEM columns a CTA holds (bounds the CTAs per SM)
+    int loge = 4;       // log2 of the samples a thread holds
+    // 32 samples a thread: the pair's own sub-pass tables (offsets into the
+    // plan's twiddle table; -1: the passes' tables are used)
+    int64_t sub_off_a = -1, sub_off_b = -1;
 };
 // Upper bound on the intermediates in flight between the two passes (bytes).
 constexpr uint64_t kFusedWindowBytes = 48ull << 20;
@@ -121,7 +125,11 @@ cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
 constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096;
 
 // fft_fused2.cu, fft_fused3.cu
-bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d);
+// loge 5: tiles of 32 samples a thread (radix-32 sub-passes), pairs with a radix-2^9/2^10 pass
+bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d, int loge = 4);
+// Sub-pass table segments of a radix-2^logr pass tile with 2^loge samples a
+// thread, offsets from `base`; sets `entries`.  Returns the segment count.
+int pass_sub_segments(int logr, int loge, TwiddleSegment *out, uint64_t base, int &entries);
 bool fused3_kernel_info(int logn, FusedDesc &d);  // passes 2-3 of (logn - 16, 8, 8)
 cudaError_t fused_prepare(FusedDesc &d);
 uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms);

@@ -144,3 +144,32 @@ def test_32_samples_per_thread_matches_16_with_load_ops(tmp_path, monkeypatch, o
         w = signals.hann_window(1 << logn)
         y = ctx.c2c_host(x, gbfft.FORWARD)
         assert oracle.rel_l2(y, oracle.fft64(x * w[None, :])) <= TOL_REL_L2
+
+
+@pytest.mark.parametrize("logn", [25, 26])
+def test_three_pass_first_pass_32_samples(tmp_path, monkeypatch, oracle, lib_built, logn):
+    """N = 2^25 / 2^26 as (L-16, 8, 8) with the first pass (radix 2^9 / 2^10)
+    run with 32 samples a thread: agrees with the 16-sample plan to FP32
+    rounding in both directions; 2^25 also against numpy's FP64 FFT."""
+    import numpy as np
+
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(1, 1 << logn, seed=990 + logn)
+    outs = {}
+    for loge in (4, 5):
+        cache = tmp_path / f"tune_{loge}.jsonl"
+        lines = []
+        for d in (gbfft.FORWARD, gbfft.INVERSE):
+            line = json.loads(_cache_line(logn, 1, d, 10, 0, loge=loge))
+            line["fused"] = 1
+            lines.append(json.dumps(line))
+        cache.write_text("\n".join(lines) + "\n")
+        monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+        with gbfft.Context(0) as ctx:
+            outs[loge] = [ctx.c2c_host(x, d) for d in (gbfft.FORWARD, gbfft.INVERSE)]
+    for a, b in zip(outs[4], outs[5]):
+        assert oracle.rel_l2(b, a) <= 1e-6
+    if logn == 25:
+        ref = np.fft.fft(x.astype(np.complex128), axis=1)
+        assert oracle.rel_l2(outs[5][0], ref) <= TOL_REL_L2

@@ -28,15 +28,18 @@
 
 namespace gbfft {
 
-template <int LOGR>
-struct PassCfg : PassTileCfg<LOGR, 1> {
-    using K = PassTileCfg<LOGR, 1>;
-    static constexpr int MINB = K::THREADS >= 1024 ? 1 : 1024 / K::THREADS;
+// LE: log2 of the samples a thread holds (4: 64 registers; 5: radix-32
+// sub-passes at 128 registers, one exchange fewer for radix 2^9 / 2^10).
+template <int LOGR, int LE = 4>
+struct PassCfg : PassTileCfg<LOGR, 1, LE> {
+    using K = PassTileCfg<LOGR, 1, LE>;
+    static constexpr int REGS = LE == 4 ? 64 : 128;
+    static constexpr int MINB = K::THREADS * REGS >= 65536 ? 1 : 65536 / (K::THREADS * REGS);
     static constexpr size_t SMEM = K::SMEM_ELEMS * sizeof(float2);
 };
 
-template <int LOGR, bool FIRST>
-__global__ void __launch_bounds__(PassCfg<LOGR>::THREADS, PassCfg<LOGR>::MINB)
+template <int LOGR, bool FIRST, int LE = 4>
+__global__ void __launch_bounds__(PassCfg<LOGR, LE>::THREADS, PassCfg<LOGR, LE>::MINB)
 fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                 const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                 float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
@@ -60,14 +63,14 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
     a.coherent_load = false;
     a.row = (uint32_t)b;
     a.ops = ops;
-    pass_tile<LOGR, 1, FIRST>(a, smem_pass);
+    pass_tile<LOGR, 1, FIRST, DftRegs, 0, -1, LE>(a, smem_pass);
 }
 
 // Persistent variant: each CTA walks tiles blockIdx.x, +gridDim.x, ... and asks
 // L2 for the next tile's R row segments (128 bytes each, one per thread)
 // before computing the current one.
-template <int LOGR, bool FIRST>
-__global__ void __launch_bounds__(PassCfg<LOGR>::THREADS, PassCfg<LOGR>::MINB)
+template <int LOGR, bool FIRST, int LE = 4>
+__global__ void __launch_bounds__(PassCfg<LOGR, LE>::THREADS, PassCfg<LOGR, LE>::MINB)
 fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                            const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops,
@@ -80,7 +83,7 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
         const uint64_t next = tile + gridDim.x;
         if (next < ntiles) {
             const float2 *nb = in + ((next / tiles_per_row) << logn) + ((next % tiles_per_row) << kColsLog);
-            for (int m = threadIdx.x; m < R; m += PassCfg<LOGR>::THREADS) prefetch_l2(nb + ((uint64_t)m << lognc));
+            for (int m = threadIdx.x; m < R; m += PassCfg<LOGR, LE>::THREADS) prefetch_l2(nb + ((uint64_t)m << lognc));
         }
         const uint64_t b = tile / tiles_per_row;
         PassArgs a;
@@ -99,7 +102,7 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
         a.coherent_load = false;
         a.row = (uint32_t)b;
         a.ops = ops;
-        pass_tile<LOGR, 1, FIRST>(a, smem_pass);
+        pass_tile<LOGR, 1, FIRST, DftRegs, 0, -1, LE>(a, smem_pass);
         __syncthreads();  // shared memory is reused by the next tile
     }
 }
@@ -108,21 +111,30 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
 // host side
 // ---------------------------------------------------------------------------
 
-template <int LOGR>
+template <int LOGR, int LE = 4>
 static void pass_describe(PassDesc &d, bool first) {
-    using C = PassCfg<LOGR>;
-    d.fn = first ? (const void *)fft_pass_kernel<LOGR, true> : (const void *)fft_pass_kernel<LOGR, false>;
-    d.fn_persistent = first ? (const void *)fft_pass_persistent_kernel<LOGR, true>
-                            : (const void *)fft_pass_persistent_kernel<LOGR, false>;
+    using C = PassCfg<LOGR, LE>;
+    d.fn = first ? (const void *)fft_pass_kernel<LOGR, true, LE> : (const void *)fft_pass_kernel<LOGR, false, LE>;
+    d.fn_persistent = first ? (const void *)fft_pass_persistent_kernel<LOGR, true, LE>
+                            : (const void *)fft_pass_persistent_kernel<LOGR, false, LE>;
     d.threads = C::THREADS;
     d.smem = C::SMEM;
     d.cols = kCols;
-    d.nseg = subcfg_segments<LOGR>(d.segs, 0);
-    d.tw_entries = SubCfg<LOGR>::tw_entries();
+    d.nseg = subcfg_segments<LOGR, LE>(d.segs, 0);
+    d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
 }
 
-bool pass_kernel_info(int logr, bool first, PassDesc &d) {
+bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge) {
     d.logr = logr;
+    if (loge == 5) {  // first passes of radix 2^9 / 2^10 (N = 2^25, 2^26 as (L-16, 8, 8))
+        if (!first) return false;
+        switch (logr) {
+            case 9: pass_describe<9, 5>(d, true); return true;
+            case 10: pass_describe<10, 5>(d, true); return true;
+            default: return false;
+        }
+    }
+    if (loge != 4) return false;
     switch (logr) {
 #define GBFFT_PASS_CASE(L) \
     case L: pass_describe<L>(d, first); return true;

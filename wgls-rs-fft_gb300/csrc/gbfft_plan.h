@@ -105,7 +105,8 @@ struct Plan {
 };
 
 // fft_passes.cu
-bool pass_kernel_info(int logr, bool first, PassDesc &d);
+// loge 5: 32 samples a thread, for the first pass of radix 2^9 / 2^10 only
+bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge = 4);
 cudaError_t pass_prepare(PassDesc &d);
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,

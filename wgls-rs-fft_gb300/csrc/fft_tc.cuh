@@ -18,9 +18,9 @@
 //   TF32 (kind::tf32): hi = x rounded to the nearest TF32 value (an integer
 //     add and mask), lo = x - hi (exact in FP32; the tensor core uses its top
 //     11 significant bits).  TF32 keeps FP32's exponent range, so no scaling
-//     is needed: three instructions per value instead of the 16-bit forms'
-//     scale, convert, convert back, subtract and convert.  About 22
-//     significant bits.
+//     is needed (three instructions per value; the 16-bit forms take a scale,
+//     and per pair of values two packed converts and two mixed-precision
+//     FMAs, plus the row maximum and the unscale).  About 22 significant bits.
 //
 // Operands live in shared memory in the canonical K-major, no-swizzle layout
 // of the tcgen05 matrix descriptors: core matrices of 8 rows x 16 bytes (8
@@ -155,22 +155,30 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// hi/lo parts of two values packed as 16-bit pairs (a in the low half):
+// hi = RN16(v), lo = RN16(v - hi).  The remainder v - hi is exact in FP32 and
+// comes from one mixed-precision FMA per value (hi * -1 + v, hi read as FP16
+// or BF16 straight from the packed pair), so a pair costs two packed converts
+// and two FMAs instead of a convert, a convert back and a subtract per value.
 template <bool BF16>
-struct TcSplit {
-    __device__ __forceinline__ static void split(float x, uint16_t &hi, uint16_t &lo) {
-        if constexpr (BF16) {
-            const __nv_bfloat16 h = __float2bfloat16_rn(x);
-            const __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
-            hi = __bfloat16_as_ushort(h);
-            lo = __bfloat16_as_ushort(l);
-        } else {
-            const __half h = __float2half_rn(x);
-            const __half l = __float2half_rn(x - __half2float(h));
-            hi = __half_as_ushort(h);
-            lo = __half_as_ushort(l);
-        }
+__device__ __forceinline__ void tc_split2(float a, float b, uint32_t &hi, uint32_t &lo) {
+    float la, lb;
+    if constexpr (BF16) {
+        asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(b), "f"(a));
+        asm("{\n\t.reg .b16 h0, h1, m;\n\tmov.b32 {h0, h1}, %2;\n\tmov.b16 m, 0xBF80;\n\t"
+            "fma.rn.f32.bf16 %0, h0, m, %3;\n\tfma.rn.f32.bf16 %1, h1, m, %4;\n\t}"
+            : "=f"(la), "=f"(lb)
+            : "r"(hi), "f"(a), "f"(b));
+        asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(lb), "f"(la));
+    } else {
+        asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(b), "f"(a));
+        asm("{\n\t.reg .b16 h0, h1, m;\n\tmov.b32 {h0, h1}, %2;\n\tmov.b16 m, 0xBC00;\n\t"
+            "fma.rn.f32.f16 %0, h0, m, %3;\n\tfma.rn.f32.f16 %1, h1, m, %4;\n\t}"
+            : "=f"(la), "=f"(lb)
+            : "r"(hi), "f"(a), "f"(b));
+        asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(lb), "f"(la));
     }
-};
+}
 
 // TF32 split: hi = x rounded to the nearest TF32 value (sign, exponent and 10
 // explicit mantissa bits; ties away from zero), lo = x - hi, exact in FP32 and
@@ -241,15 +249,8 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
         uint32_t hi[16], lo[16];
 #pragma unroll
         for (int e = 0; e < 16; e += 2) {
-            uint16_t h0, l0, h1, l1;
-            TcSplit<BF16>::split(x[e].x * down, h0, l0);
-            TcSplit<BF16>::split(x[e + 1].x * down, h1, l1);
-            hi[e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-            lo[e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
-            TcSplit<BF16>::split(x[e].y * down, h0, l0);
-            TcSplit<BF16>::split(x[e + 1].y * down, h1, l1);
-            hi[8 + e / 2] = (uint32_t)h0 | ((uint32_t)h1 << 16);
-            lo[8 + e / 2] = (uint32_t)l0 | ((uint32_t)l1 << 16);
+            tc_split2<BF16>(x[e].x * down, x[e + 1].x * down, hi[e / 2], lo[e / 2]);
+            tc_split2<BF16>(x[e].y * down, x[e + 1].y * down, hi[8 + e / 2], lo[8 + e / 2]);
         }
 #pragma unroll
         for (int kb = 0; kb < 4; ++kb) {  // 4 chunks of 8 K-values (16 bytes)

@@ -173,3 +173,29 @@ def test_three_pass_first_pass_32_samples(tmp_path, monkeypatch, oracle, lib_bui
     if logn == 25:
         ref = np.fft.fft(x.astype(np.complex128), axis=1)
         assert oracle.rel_l2(outs[5][0], ref) <= TOL_REL_L2
+
+
+@pytest.mark.parametrize("logn,batch,loge", [(21, 3, 4), (22, 2, 4), (25, 1, 5)])
+def test_three_pass_persistent_first_pass(tmp_path, monkeypatch, oracle, lib_built, logn, batch, loge):
+    """Three-pass plans whose lone first pass runs as a persistent tile loop
+    (L2 prefetch of the next tile), the last two passes fused: FP64 gate in
+    both directions."""
+    import numpy as np
+
+    import gbfft
+    from gbfft import signals
+    cache = tmp_path / "tune.jsonl"
+    lines = []
+    for d in (gbfft.FORWARD, gbfft.INVERSE):
+        line = json.loads(_cache_line(logn, batch, d, 10, 1, loge=loge))
+        line["fused"] = 1
+        lines.append(json.dumps(line))
+    cache.write_text("\n".join(lines) + "\n")
+    monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+    x = signals.normal_c64(batch, 1 << logn, seed=1000 + logn)
+    with gbfft.Context(0) as ctx:
+        y = ctx.c2c_host(x, gbfft.FORWARD)
+        z = ctx.c2c_host(y, gbfft.INVERSE)
+    ref = np.fft.fft(x.astype(np.complex128), axis=1)
+    assert oracle.rel_l2(y, ref) <= TOL_REL_L2
+    assert oracle.rel_l2(z, x) <= 1e-6

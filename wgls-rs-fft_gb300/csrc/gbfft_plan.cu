@@ -107,8 +107,12 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         // its first pass with 32 samples a thread where that exists (radix 2^9 /
         // 2^10: N = 2^25, 2^26), measured faster (2^26: 114.9 vs 112.9 GSa/s)
         PassDesc pd;
-        if (pass_kernel_info(logn - 16, true, pd, 5)) c.push_back(PlanVariant{10, false, true, 0, 5});
+        const bool e32 = pass_kernel_info(logn - 16, true, pd, 5);
+        if (e32) c.push_back(PlanVariant{10, false, true, 0, 5});
         c.push_back(PlanVariant{10, false, true});
+        // the lone first pass as a persistent tile loop with L2 prefetch of the next tile
+        if (e32) c.push_back(PlanVariant{10, true, true, 0, 5});
+        c.push_back(PlanVariant{10, true, true});
     }
     for (int m = top; m >= 7; --m) {
         const std::vector<int> parts = split_passes(logn, m);
@@ -271,8 +275,8 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
             if (st != GBFFT_OK) return st;
             const PassDesc &d0 = p.passes[0];
             e = pass_launch(d0, in, (float2 *)ws.ptr, batch, p.logn, p.tw + d0.sub_tw_offset, p.tw + p.tw_lo_offset,
-                            p.tw + p.tw_hi_offset, p.tw_split, inv ? -1.0f : 1.0f, 1.0f, 1.0f, stream, false, p.sms,
-                            ops);
+                            p.tw + p.tw_hi_offset, p.tw_split, inv ? -1.0f : 1.0f, 1.0f, 1.0f, stream,
+                            p.variant.persistent, p.sms, ops);
             if (e != cudaSuccess) {
                 why = cudaGetErrorString(e);
                 return GBFFT_ERR_CUDA;

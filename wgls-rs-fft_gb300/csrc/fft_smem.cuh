@@ -54,7 +54,7 @@ struct SubCfg {
 
 // a * W_16^I for a compile-time I (exact special cases where they exist).
 template <int I>
-__device__ __forceinline__ float2 mul_w16c(float2 a) {
+GBFFT_HD float2 mul_w16c(float2 a) {
     constexpr int i = I & 15;
     if constexpr (i == 0) return a;
     else if constexpr (i == 1) return mul_w16_1(a);
@@ -80,7 +80,7 @@ constexpr float kSin1_32 = 0.19509032201612826785f;  // sin(pi/16)
 constexpr float kCos3_32 = 0.83146961230254523708f;  // cos(3 pi/16)
 constexpr float kSin3_32 = 0.55557023301960222474f;  // sin(3 pi/16)
 template <int I>
-__device__ __forceinline__ float2 mul_w32c(float2 a) {
+GBFFT_HD float2 mul_w32c(float2 a) {
     constexpr int i = I & 31;
     if constexpr ((i & 1) == 0) return mul_w16c<i / 2>(a);
     else if constexpr (i > 8) return mul_mi(mul_w32c<i - 8>(a));  // W_32^8 = -i
@@ -94,7 +94,7 @@ __device__ __forceinline__ float2 mul_w32c(float2 a) {
 
 // 32-point DFT: radix-2 decimation in frequency, then two 16-point DFTs.
 template <> struct Dft<32> {
-    __device__ __forceinline__ static void run(float2 *x) {
+    GBFFT_HD static void run(float2 *x) {
         float2 a[16], b[16];
         auto split = [&](auto kc) {
             constexpr int k = decltype(kc)::value;

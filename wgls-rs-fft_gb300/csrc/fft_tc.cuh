@@ -65,16 +65,7 @@ struct TcGeom {
     }
 };
 
-// 16-bit kinds (unchanged users of the older names)
-constexpr int kTcRowBytes = TcGeom<kTcF16>::ROW_BYTES;
-constexpr int kTcGBytes = TcGeom<kTcF16>::G_BYTES;
-
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Byte offset of element (row, k) in a 16-bit K-major no-swizzle operand.
-__host__ __device__ __forceinline__ uint32_t tc_elem_offset(uint32_t row, uint32_t k) {
-    return TcGeom<kTcF16>::elem_offset(row, k);
-}
 
 // tcgen05 shared-memory matrix descriptor (no swizzle, K-major).
 __device__ __forceinline__ uint64_t tc_smem_desc(uint32_t saddr, uint32_t sbo) {

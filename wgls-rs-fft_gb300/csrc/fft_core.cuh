@@ -12,6 +12,12 @@
 // Butterfly building blocks are host and device functions (the host side
 // only serves the CPU tests that check them against an FP64 DFT).
 #define GBFFT_HD __host__ __device__ __forceinline__
+// loop unrolling hint for code that is also compiled for the host
+#if defined(__CUDA_ARCH__)
+#define GBFFT_UNROLL _Pragma("unroll")
+#else
+#define GBFFT_UNROLL
+#endif
 
 namespace gbfft {
 
@@ -79,7 +85,7 @@ template <> struct Dft<8> {
     // applied without k; the second 4-point DFT's last additions take k as FMAs.
     GBFFT_HD static void run(float2 *x) {
         float2 a[4], b[4];
-#pragma unroll
+        GBFFT_UNROLL
         for (int k = 0; k < 4; ++k) {
             a[k] = cadd(x[k], x[k + 4]);
             b[k] = csub(x[k], x[k + 4]);
@@ -118,11 +124,11 @@ template <> struct Dft<16> {
     // instructions each: 144 instructions for the 16-point DFT instead of 160.
     GBFFT_HD static void run(float2 *x) {
         float2 z[4][4];
-#pragma unroll
+        GBFFT_UNROLL
         for (int n1 = 0; n1 < 4; ++n1) {
             float2 t[4] = {x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]};
             Dft<4>::run(t);
-#pragma unroll
+            GBFFT_UNROLL
             for (int k2 = 0; k2 < 4; ++k2) z[n1][k2] = t[k2];
         }
         {  // k2 = 0: no twiddles

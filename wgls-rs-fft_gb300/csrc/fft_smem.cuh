@@ -106,7 +106,7 @@ template <> struct Dft<32> {
         }(std::make_integer_sequence<int, 16>{});
         Dft<16>::run(a);
         Dft<16>::run(b);
-#pragma unroll
+        GBFFT_UNROLL
         for (int k = 0; k < 16; ++k) {
             x[2 * k] = a[k];
             x[2 * k + 1] = b[k];

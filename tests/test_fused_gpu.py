@@ -195,11 +195,12 @@ def test_fused_radix128_pair_for_single_pass_sizes(torch, oracle, lib_built, tmp
         assert oracle.rel_l2(yf, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2
 
 
-@pytest.mark.parametrize("logn,batch", [(17, 1), (17, 33), (18, 5), (18, 40), (19, 3), (20, 2), (20, 9)])
+@pytest.mark.parametrize("logn,batch", [(15, 3), (16, 7), (17, 1), (17, 33), (18, 5), (18, 40), (19, 3), (20, 2),
+                                        (20, 9)])
 def test_fused_32_samples_per_thread(torch, oracle, lib_built, tmp_path, monkeypatch, logn, batch):
     """The pass pair with 32 samples a thread (radix-32 sub-passes: a
     radix-2^9 pass as 32 x 16 instead of 16 x 16 x 2, 2^10 as 32 x 32 instead
-    of 16 x 16 x 4), with its own sub-pass tables: FP64 gate, agreement with
+    of 16 x 16 x 4, 2^8 as 32 x 8, 2^7 as 32 x 4), with its own sub-pass tables: FP64 gate, agreement with
     the 16-sample pair to FP32 rounding, repeated launches, noise on load."""
     import gbfft
     from gbfft import signals

@@ -13,6 +13,8 @@ bool fused2_kernel_info(int logr1, int logr2, FusedDesc &d, int loge) {
     if (loge == 5) {
 #define GBFFT_F2E(A, B, T) \
     if (logr1 == A && logr2 == B) { fused_describe<A, B, T, A + B, 0, 5>(d); return true; }
+        GBFFT_F2E(8, 7, 128)
+        GBFFT_F2E(8, 8, 128)
         GBFFT_F2E(9, 8, 256)
         GBFFT_F2E(9, 9, 256)
         GBFFT_F2E(10, 9, 512)
@@ -39,7 +41,7 @@ int pass_sub_segments(int logr, int loge, TwiddleSegment *out, uint64_t base, in
     switch (loge * 16 + logr) {
 #define GBFFT_SEG(E, R) \
     case E * 16 + R: entries = SubCfg<R, E>::tw_entries(); return subcfg_segments<R, E>(out, base);
-        GBFFT_SEG(5, 8) GBFFT_SEG(5, 9) GBFFT_SEG(5, 10)
+        GBFFT_SEG(5, 7) GBFFT_SEG(5, 8) GBFFT_SEG(5, 9) GBFFT_SEG(5, 10)
         GBFFT_SEG(4, 5) GBFFT_SEG(4, 6) GBFFT_SEG(4, 7) GBFFT_SEG(4, 8) GBFFT_SEG(4, 9) GBFFT_SEG(4, 10)
 #undef GBFFT_SEG
         default: entries = 0; return -1;

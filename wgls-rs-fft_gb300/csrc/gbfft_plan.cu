@@ -119,14 +119,17 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         bool dup = false;
         for (const PlanVariant &v : c) dup |= split_passes(logn, v.max_logr) == parts;
         if (dup || parts[0] < 5) continue;
-        // the pair with 32 samples a thread (radix-32 sub-passes) first where it
-        // exists: measured faster at 2^17..2^20 (177 / 178.5 / 150.7 / 155.9
-        // against 174.7 / 166.2 / 145.6 / 144.7 GSa/s)
-        if (!tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd, 5))
-            c.push_back(PlanVariant{m, false, true, 0, 5});
+        // the pair with 32 samples a thread (radix-32 sub-passes) first where a
+        // pass has radix 2^9 or more: measured faster at 2^17..2^20 (177 / 178.5 /
+        // 150.7 / 155.9 against 174.7 / 166.2 / 145.6 / 144.7 GSa/s); after the
+        // 16-sample pair otherwise
+        const bool e32 = !tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd, 5);
+        const bool e32_first = e32 && parts[0] >= 9;
+        if (e32_first) c.push_back(PlanVariant{m, false, true, 0, 5});
         if (parts.size() == 2 && (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, fd)
                                      : fused2_kernel_info(parts[0], parts[1], fd)))
             c.push_back(PlanVariant{m, false, true});
+        if (e32 && !e32_first) c.push_back(PlanVariant{m, false, true, 0, 5});
         c.push_back(PlanVariant{m, false});
         if (!tc) c.push_back(PlanVariant{m, true});
     }

@@ -199,3 +199,23 @@ def test_three_pass_persistent_first_pass(tmp_path, monkeypatch, oracle, lib_bui
     ref = np.fft.fft(x.astype(np.complex128), axis=1)
     assert oracle.rel_l2(y, ref) <= TOL_REL_L2
     assert oracle.rel_l2(z, x) <= 1e-6
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (3, 2e-6)])
+def test_autotune_split_form(tmp_path, monkeypatch, oracle, lib_built, prec, tol):
+    """The tuner at a split precision times the split form's own candidates
+    (fused pass pair, one launch per pass), caches the choice under that
+    precision, and the chosen plan meets the form's FP64 gate."""
+    import gbfft
+    from gbfft import signals
+    cache = tmp_path / "tune.jsonl"
+    monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+    n, batch = 1 << 16, 8
+    x = signals.tones_c64(batch, n, seed=77)
+    with gbfft.Context(0) as ctx:
+        ctx.set_precision(prec)
+        assert ctx.autotune(n, batch, gbfft.FORWARD) > 0
+        y = ctx.c2c_host(x, gbfft.FORWARD)
+    assert oracle.rel_l2(y, oracle.fft64(x)) <= tol
+    lines = [json.loads(l) for l in cache.read_text().splitlines()]
+    assert len(lines) == 1 and lines[0]["precision"] == prec and lines[0]["logn"] == 16

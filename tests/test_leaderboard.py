@@ -76,19 +76,21 @@ NCU_CSV = '''==PROF== Connected to process 1
 "1","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","dram__bytes_write.sum","byte","8388608"
 "1","7","python3.12","h","void gbfft::fft_rows_kernel<10, 11>(const float2 *, float2 *)","1","7","(128, 1, 1)","(512, 1, 1)","0","10.3","Command line profiler metrics","gpu__time_duration.sum","us","6"
 "2","7","python3.12","h","void gbfft::twiddle_fill_kernel(float2 *)","1","7","(256, 1, 1)","(4, 1, 1)","0","10.3","Command line profiler metrics","gpu__time_duration.sum","ns","1500"
+"3","7","python3.12","h","void fft_rows_kernel<12, 12, (int)-1, 4>(const float2 *, float2 *)","1","7","(256, 1, 1)","(8, 1, 1)","0","10.3","Command line profiler metrics","gpu__time_duration.sum","ns","900"
 '''
 
 
 def test_parse_ncu_csv_aggregates_per_kernel(lib_built):
     from gbfft import leaderboard as lb
     ks = lb.parse_ncu_csv(NCU_CSV)
-    assert [k.kernel for k in ks] == ["gbfft::fft_rows_kernel<10, 11>", "gbfft::twiddle_fill_kernel"]
+    assert [k.kernel for k in ks] == ["gbfft::fft_rows_kernel<10, 11>", "gbfft::twiddle_fill_kernel",
+                                      "fft_rows_kernel<12, 12, (int)-1, 4>"]
     rows = ks[0]
     assert rows.launches == 2 and rows.seconds == pytest.approx(10e-6) and rows.dram_bytes == 4 * 8388608
     assert ks[1].launches == 1 and ks[1].dram_bytes == 0
     assert lb.parse_ncu_csv("no csv here") == []
     text = lb.format_counters(1024, 1024, "GB300 FP32", ks)
-    assert "2 launch" not in text and "3 launch(es)" in text and "fft_rows_kernel" in text
+    assert "4 launch(es)" in text and "fft_rows_kernel" in text
 
 
 def test_ncu_counters_runs_plain_first_then_ncu(lib_built, tmp_path):

@@ -223,7 +223,9 @@ def parse_ncu_csv(text: str) -> List[KernelCounters]:
         per_launch.setdefault((row["ID"], row["Kernel Name"]), {})[metric] = value
     out = {}
     for (_, name), rec in per_launch.items():
-        short = name.split("(")[0].replace("void ", "").strip()
+        # drop the parameter list: it starts after the template's closing '>'
+        # (template arguments may hold parentheses themselves, e.g. "(int)-1")
+        short = (name[:name.index(">(") + 1] if ">(" in name else name.split("(")[0]).replace("void ", "").strip()
         k = out.setdefault(short, KernelCounters(short, 0, 0.0, 0.0))
         k.launches += 1
         k.seconds += rec.get("gpu__time_duration.sum", 0.0)

@@ -146,6 +146,9 @@ typedef struct gbfft_ragged_plan gbfft_ragged_plan;
 /* Options for gbfft_ragged_plan_set. */
 #define GBFFT_RAGGED_OPT_SPIN_LIMIT 1          /* polls before a dependency wait gives up */
 #define GBFFT_RAGGED_OPT_TEST_DROP_PRODUCERS 2 /* test hook: omit first-pass items */
+#define GBFFT_RAGGED_OPT_LAG 3                 /* queue distance from a transform's first-pass items to its
+                                                  second-pass items, in items per SM (1..64, default 4):
+                                                  larger waits less, smaller keeps the intermediate in L2 */
 
 /* Build the work queue, twiddle tables and workspace for a descriptor set
  * (validated here; errors are reported on `ctx`). */

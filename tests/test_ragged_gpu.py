@@ -234,3 +234,28 @@ def test_ragged_split_form_wait_times_out(lib_built, torch):
         plan.close()
         ctx.set_precision(gbfft.PREC_FP32)
         assert np.isfinite(ctx.c2c_host(x[:256][None, :], gbfft.FORWARD)).all()
+
+
+def test_ragged_lag_option(lib_built, torch):
+    """GBFFT_RAGGED_OPT_LAG only reorders the work queue: every lag gives the
+    same bits; values outside 1..64 are refused."""
+    import gbfft
+    from gbfft import signals
+    descs, total = _mixed_descs([16, 18, 10, 17, 12, 15], [-1, 1, 1, -1, -1, 1])
+    x = signals.uniform_c64(1, total, seed=47)[0]
+    with gbfft.Context(0) as ctx:
+        d = torch.from_numpy(x).cuda()
+        outs = []
+        plan = ctx.ragged_plan(descs)
+        for lag in (4, 1, 16):
+            plan.set(gbfft.RAGGED_OPT_LAG, lag)
+            o = torch.full_like(d, float("nan"))
+            plan.execute(d, o, total, use_graph=True)
+            plan.wait()
+            outs.append(o.cpu().numpy())
+        for v in (0, 65):
+            with pytest.raises(gbfft.GbfftError) as e:
+                plan.set(gbfft.RAGGED_OPT_LAG, v)
+            assert e.value.status == gbfft.ERR_INVALID_ARGUMENT
+        plan.close()
+    assert np.array_equal(outs[0], outs[1], equal_nan=True) and np.array_equal(outs[0], outs[2], equal_nan=True)

@@ -315,6 +315,7 @@ struct RaggedPlanImpl {
     uint64_t max_extent = 0;  // one past the last sample any transform touches
     uint32_t spin_limit = 1u << 22;
     bool drop_producers = false;
+    uint32_t lag_per_sm = 4;  // GBFFT_RAGGED_OPT_LAG
     bool dirty = true;        // items must be (re)uploaded
     std::vector<RagXform> xf;
     std::vector<RagItem> items;
@@ -390,7 +391,7 @@ static void build_items(RaggedPlanImpl &p) {
     uint64_t total_p1 = 0;
     for (uint32_t i : two) total_p1 += p.xf[i].tiles1;
     // the second pass of a transform follows its first pass by `lag` items
-    const uint64_t lag = 4ull * (uint64_t)std::max(1, p.sms);
+    const uint64_t lag = (uint64_t)p.lag_per_sm * (uint64_t)std::max(1, p.sms);
     std::vector<std::pair<uint32_t, uint64_t>> pending;  // (transform, release position), FIFO
     size_t head = 0, ri = 0;
     uint64_t p1_seen = 0;
@@ -675,6 +676,14 @@ int ragged_plan_set(RaggedPlanImpl &p, int option, uint64_t value, std::string &
             break;
         case GBFFT_RAGGED_OPT_TEST_DROP_PRODUCERS:
             p.drop_producers = value != 0;
+            build_items(p);
+            break;
+        case GBFFT_RAGGED_OPT_LAG:
+            if (value < 1 || value > 64) {
+                why = "lag must be in [1, 64] items per SM";
+                return GBFFT_ERR_INVALID_ARGUMENT;
+            }
+            p.lag_per_sm = (uint32_t)value;
             build_items(p);
             break;
         default:

@@ -272,3 +272,4 @@ class RaggedPlan:
 
 RAGGED_OPT_SPIN_LIMIT = 1
 RAGGED_OPT_TEST_DROP_PRODUCERS = 2
+RAGGED_OPT_LAG = 3

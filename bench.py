@@ -148,10 +148,27 @@ class ClockSampler:
         if self._t:
             self._t.join(timeout=2)
 
-    def summary(self):
+    def count_since(self, t0: float) -> int:
+        return sum(1 for t, _ in self.lines if t >= t0)
+
+    def keep_busy(self, t0: float, step, sync, want: int = 3, max_s: float = 2.0):
+        """When the timed region was too short for `want` samples after t0,
+        repeat `step` (outside the timed region) until they arrive, so the
+        clocks are read with the GPU under the same load."""
+        if not self.proc:
+            return
+        deadline = time.time() + max_s
+        while self.count_since(t0) < want and time.time() < deadline:
+            for _ in range(4):
+                step()
+            sync()
+
+    def summary(self, t0: float = 0.0):
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for _, line in self.lines:
+        for t, line in self.lines:
+            if t < t0:  # before the GPU was busy
+                continue
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -283,6 +300,7 @@ def run_ragged(args, ctx, dev, rank, world):
     sp = stream.cuda_stream
     sampler = ClockSampler(dev.index or 0)
     sampler.start()
+    t_busy = time.time()
     for _ in range(args.warmup):
         plan.execute(x, y, total, use_graph=True, stream=sp)
     plan.wait(stream=sp)
@@ -298,9 +316,11 @@ def run_ragged(args, ctx, dev, rank, world):
     ev1.record(stream)
     torch.cuda.nvtx.range_pop()
     plan.wait(stream=sp)
+    launches = plan.launch_count() - l0
+    sampler.keep_busy(t_busy, lambda: plan.execute(x, y, total, use_graph=True, stream=sp),
+                      lambda: plan.wait(stream=sp))
     sampler.stop()
     ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
-    launches = plan.launch_count() - l0
     value = total * args.steps * world / (ms * 1e-3) / 1e9
 
     # uniform-batch comparison: same transforms regrouped by (size, direction)
@@ -371,7 +391,7 @@ def run_ragged(args, ctx, dev, rank, world):
             "uniform_batches": {"value": uvalue, "unit": UNIT, "launches_per_step": len(calls),
                                 "ragged_over_uniform": value / uvalue},
             "cpu_baseline": None, "e2e": None, "gpu_launches": launches,
-            "clocks": sampler.summary(),
+            "clocks": sampler.summary(t_busy),
             "accuracy": {"precision": args.precision, "max_rel_l2_vs_fp64": worst, "sizes_checked": len(seen),
                          "reference": "float64 torch.fft of one transform per size (checker only)"},
         }
@@ -439,6 +459,7 @@ def main():
 
     sampler = ClockSampler(local)
     sampler.start()
+    t_busy = time.time()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize(dev)
@@ -454,10 +475,12 @@ def main():
     ev1.record(stream)
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize(dev)
+    launches = ctx.launch_count() - launches0
+    # short timed regions: clocks are read while the same steps keep running
+    sampler.keep_busy(t_busy, step, lambda: torch.cuda.synchronize(dev))
     sampler.stop()
     if world > 1:
         torch.distributed.barrier()
-    launches = ctx.launch_count() - launches0
     ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
     samples_per_step = 2 * n * batch
     value = samples_per_step * args.steps * world / (ms * 1e-3) / 1e9
@@ -569,7 +592,7 @@ def main():
             "gflops": value * 5 * logn,  # 5 N log2 N flops per transform (the reference's model)
             "e2e": e2e,
             "gpu_launches": launches,
-            "clocks": sampler.summary(),
+            "clocks": sampler.summary(t_busy),
             "roundtrip_rel_l2": rt,
             "accuracy": {"precision": args.precision, "rel_l2_vs_fp64": acc, "rows": acc_rows,
                          "reference": "float64 torch.fft of the sampled rows (checker only)"},

@@ -52,7 +52,7 @@ typedef enum gbfft_precision {
     GBFFT_PREC_FP32 = 0,      /* plain FP32 Stockham form (every size) */
     GBFFT_PREC_TC_FP16 = 1,   /* radix-16 sub-DFTs as tcgen05 matrix products, FP16 hi+lo operands
                                  (3 products), per-vector power-of-two scaling, FP32 accumulation;
-                                 multi-pass sizes N >= 2^15 */
+                                 N >= 16 (TF32: single-pass sizes up to 2^13, then N >= 2^15) */
     GBFFT_PREC_TC_BF16X3 = 2, /* same with BF16 hi+lo operands */
     GBFFT_PREC_TC_TF32 = 3    /* same with TF32 hi+lo operands (hi = the value rounded to TF32,
                                  lo = the exact rest); TF32 keeps FP32's exponent range, so no

@@ -58,11 +58,8 @@ def test_leaderboard_rivals_pass_on_gpu(lib_built, capsys):
     for n in (1024, 65536):
         results = [lb.run_rival(r, n, lb.choose_batch_size(n)) for r in rivals]
         for res in results:
-            if res.name.startswith("GB300 split") and n < (1 << 15):
-                assert res.status == gbfft.status_string(gbfft.ERR_UNSUPPORTED)
-            else:
-                assert res.status == "PASS", (n, res)
-                assert res.msamples_per_sec > 0
+            assert res.status == "PASS", (n, res)
+            assert res.msamples_per_sec > 0
     assert lb.main(["--sizes", "256"]) == 0
     assert "RIVALRY LEADERBOARD" in capsys.readouterr().out
 

@@ -394,10 +394,11 @@ def test_small_sizes_every_batch(gpu_ctx, oracle, logn):
 def test_precision_from_environment(lib_built, monkeypatch):
     import gbfft
     monkeypatch.setenv("GBFFT_PRECISION", "tc_fp16")
-    with gbfft.Context(0) as ctx:  # the split form covers N >= 2^15 only
+    with gbfft.Context(0) as ctx:  # the split form needs N >= 16 (one radix-16 sub-pass)
         with pytest.raises(gbfft.GbfftError) as e:
-            ctx.c2c_host(np.ones((1, 256), np.complex64), gbfft.FORWARD)
+            ctx.c2c_host(np.ones((1, 8), np.complex64), gbfft.FORWARD)
         assert e.value.status == gbfft.ERR_UNSUPPORTED
+        assert np.allclose(ctx.c2c_host(np.ones((1, 256), np.complex64), gbfft.FORWARD)[0][0], 256)
     monkeypatch.delenv("GBFFT_PRECISION")
     with gbfft.Context(0) as ctx:
         assert np.allclose(ctx.c2c_host(np.ones((1, 256), np.complex64), gbfft.FORWARD)[0][0], 256)

@@ -70,8 +70,12 @@ def test_tc_matches_fp32_form_and_limits(tc_ctx, oracle):
     tc_ctx.set_precision(gbfft.PREC_TC_FP16)
     ytc = tc_ctx.c2c_host(x, gbfft.FORWARD)
     assert oracle.rel_l2(ytc, y32) <= 2e-6
-    with pytest.raises(gbfft.GbfftError) as e:  # single-pass sizes stay FP32-only
-        tc_ctx.c2c_host(signals.uniform_c64(2, 4096, seed=1), gbfft.FORWARD)
+    with pytest.raises(gbfft.GbfftError) as e:  # below one radix-16 sub-pass
+        tc_ctx.c2c_host(signals.uniform_c64(2, 8, seed=1), gbfft.FORWARD)
+    assert e.value.status == gbfft.ERR_UNSUPPORTED
+    tc_ctx.set_precision(gbfft.PREC_TC_TF32)
+    with pytest.raises(gbfft.GbfftError) as e:  # TF32 operands of a 2^14 transform exceed shared memory
+        tc_ctx.c2c_host(signals.uniform_c64(1, 1 << 14, seed=1), gbfft.FORWARD)
     assert e.value.status == gbfft.ERR_UNSUPPORTED
     with pytest.raises(gbfft.GbfftError) as e:
         tc_ctx.set_precision(7)
@@ -111,3 +115,29 @@ def test_tc_fused_pair_matches_two_launches(lib_built, oracle, prec, tol, logn, 
             assert oracle.rel_l2(fused, ref) <= tol, (inv, oracle.rel_l2(fused, ref))
             assert oracle.rel_l2(two, ref) <= tol
             assert oracle.rel_l2(fused, two) <= 1e-6
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6)])
+@pytest.mark.parametrize("logn", list(range(4, 15)))
+def test_tc_single_pass_sizes(tc_ctx, oracle, prec, tol, logn):
+    """The split form's single-pass kernel (N = 2^4 .. 2^14; TF32 up to 2^13):
+    FP64 gate in both directions on N(0,1) rows, batches not a multiple of the
+    transforms a CTA takes, and the reference path's 1e-3 gate on the
+    reference's benchmark input."""
+    import gbfft
+    from gbfft import signals
+    if prec == 3 and logn == 14:
+        pytest.skip("TF32 single pass stops at 2^13")
+    tc_ctx.set_precision(prec)
+    n = 1 << logn
+    batch = max(1, (1 << 12) // n) + 3
+    x = signals.normal_c64(batch, n, seed=1100 + logn)
+    for direction, inv in ((gbfft.FORWARD, False), (gbfft.INVERSE, True)):
+        y = tc_ctx.c2c_host(x, direction)
+        err = oracle.rel_l2(y, oracle.fft64(x, inverse=inv))
+        assert err <= tol, (logn, inv, err)
+    # the reference's 1e-3 gate on its own benchmark input (src/benchmark.rs:204-217)
+    t = np.arange(n, dtype=np.float64) / n
+    xb = np.tile((0.001 * t + 1j * 0.001 * np.sin(2 * np.pi * t)).astype(np.complex64), (3, 1))
+    assert oracle.max_abs_err(tc_ctx.c2c_host(xb, gbfft.FORWARD), oracle.ref_fft(xb)) <= 1e-3
+    tc_ctx.set_precision(gbfft.PREC_FP32)

@@ -76,6 +76,10 @@ uint64_t multipass_segments(int logn, std::vector<PassDesc> &passes, uint64_t of
 
 std::vector<PlanVariant> plan_candidates(int logn, int precision) {
     std::vector<PlanVariant> c;
+    if (logn <= kRowsMaxLogN && precision != GBFFT_PREC_FP32) {
+        c.push_back(PlanVariant{10});  // the split form's single-pass kernel
+        return c;
+    }
     if (logn <= kRowsMaxLogN) {
         // 2^11 samples per CTA (128 threads, 8 CTAs per SM) measured fastest
         // where a transform fits (N = 2^6 .. 2^11); one CTA per SM leaves no
@@ -145,14 +149,31 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
     std::vector<TwiddleSegment> segs;
     cudaError_t e;
     const bool tc = precision != GBFFT_PREC_FP32;
-    if (tc && logn <= kRowsMaxLogN) {
-        why = "the tensor-core split form covers N >= 2^15 (multi-pass transforms)";
-        return GBFFT_ERR_UNSUPPORTED;
-    }
     // N = 2^13, 2^14 may also run as a fused two-pass transform of radix-128
     // tiles (a tuner candidate)
     const bool small_fused = v.fused && !tc && (logn == 13 || logn == 14);
-    if (logn <= kRowsMaxLogN && !small_fused) {
+    if (tc && logn <= kRowsMaxLogN) {
+        if (!rows_tc_kernel_info(logn, precision, p.rows)) {
+            why = logn < 4 ? "the tensor-core split form needs N >= 16 (one radix-16 sub-pass)"
+                           : "the TF32 split form runs single-pass sizes up to N = 2^13 (256 B of operands a thread)";
+            return GBFFT_ERR_UNSUPPORTED;
+        }
+        if ((e = rows_tc_prepare(p.rows)) != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+        segs.assign(p.rows.segs, p.rows.segs + p.rows.nseg);
+        p.tw_entries = p.rows.tw_entries;
+        if ((e = cudaMalloc(&p.gtab, kTcGtabBytes)) != cudaSuccess) {
+            cudaGetLastError();
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_OUT_OF_MEMORY;
+        }
+        if ((e = tc_gtab_fill(p.gtab, stream)) != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+    } else if (logn <= kRowsMaxLogN && !small_fused) {
         if (!rows_kernel_info(logn, p.rows, v.tile ? v.tile : 12, v.loge)) {
             why = "no single-pass kernel";
             return GBFFT_ERR_UNSUPPORTED;
@@ -302,7 +323,10 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
         return GBFFT_OK;
     }
     if (!p.multipass) {
-        e = rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.variant.persistent, p.sms, stream, ops);
+        e = p.precision != GBFFT_PREC_FP32
+                ? rows_tc_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.gtab, err, stream, ops)
+                : rows_launch(p.rows, in, out, batch, p.tw, direction, p.logn, p.variant.persistent, p.sms, stream,
+                              ops);
         if (e != cudaSuccess) {
             why = cudaGetErrorString(e);
             return GBFFT_ERR_CUDA;

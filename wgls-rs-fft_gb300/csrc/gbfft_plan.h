@@ -122,6 +122,13 @@ cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uin
                            float in_im_sign, float out_re_scale, float out_im_scale, const void *gtab,
                            uint32_t *err, cudaStream_t stream, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 cudaError_t tc_gtab_fill(void *out, cudaStream_t stream);
+
+// fft_rows_tc.cu (split form of the single-pass transform, N = 2^4 .. 2^14; TF32 up to 2^13)
+bool rows_tc_kernel_info(int logn, int precision, RowsKernelInfo &k);
+cudaError_t rows_tc_prepare(RowsKernelInfo &k);
+cudaError_t rows_tc_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
+                           const float2 *tw, int direction, int logn, const void *gtab, uint32_t *err,
+                           cudaStream_t stream, LoadOps ops);
 // G table: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (2 KB each), [TF32 hi | TF32 lo] (4 KB each)
 constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096;
 

@@ -16,7 +16,7 @@ baseline is numpy's FFT in float64 of the same input.
 
 Rivals:
   * GB300 FP32            -- gbfft.GpuFft, the reference's GpuFft interface
-  * GB300 split FP16      -- the tensor-core split form (N >= 2^15)
+  * GB300 split FP16      -- the tensor-core split form (N >= 16)
   * cuFFT (torch.fft)     -- batched C2C over the whole batch in one call
     (the reference's cuFFT wrapper plans batch = 1 and loops,
     src/cufft_wrapper.rs:49-54)
@@ -120,7 +120,7 @@ class TorchCuFft(FftExecutor):
 
 class SplitFormGpuFft(GpuFft):
     """GpuFft with the tensor-core split form (FP16 hi + lo) selected
-    (covers N >= 2^15; smaller sizes report UNSUPPORTED)."""
+    (covers N >= 16; smaller sizes report UNSUPPORTED)."""
 
     def __init__(self, device: int = 0):
         super().__init__(device)

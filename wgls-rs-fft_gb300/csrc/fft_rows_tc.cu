@@ -1,12 +1,14 @@
-// Split-precision tensor-core form of the single-pass transform (N = 2^4 .. 2^14).
+// Split-precision tensor-core form of the single-pass transform (N = 2^4 .. 2^14),
+// replacing, like fft_rows.cu, the reference's per-stage global passes
+// (larsjoost/wgls-rs-fft src/shaders.rs:8-106, dispatched by src/lib.rs:582-628).
 //
 // The same tile as fft_rows.cu -- G whole transforms a CTA, 16 samples a
 // thread, radix-16 sub-passes with shared-memory exchanges, one HBM read and
 // one write per sample -- with every radix-16 butterfly set run on the tcgen05
 // tensor cores (fft_tc.cuh; the radix 2/4/8 remainder stays on the FP32
 // pipes).  One CTA per tile (4096 samples; one transform for N = 2^13, 2^14):
-// TMEM, the mbarrier and the G parts are set up per CTA (tc_cta_setup in
-// fft_passes_tc.cu's pattern), and every completion wait is bounded.
+// TMEM, the mbarrier and the G parts are set up per CTA (as in
+// fft_passes_tc.cu), and every completion wait is bounded.
 // TF32 needs 256 B of operands per thread, so it stops at N = 2^13.
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"

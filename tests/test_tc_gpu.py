@@ -141,3 +141,44 @@ def test_tc_single_pass_sizes(tc_ctx, oracle, prec, tol, logn):
     xb = np.tile((0.001 * t + 1j * 0.001 * np.sin(2 * np.pi * t)).astype(np.complex64), (3, 1))
     assert oracle.max_abs_err(tc_ctx.c2c_host(xb, gbfft.FORWARD), oracle.ref_fft(xb)) <= 1e-3
     tc_ctx.set_precision(gbfft.PREC_FP32)
+
+
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5)])
+@pytest.mark.parametrize("logn,batch", [(15, 3), (16, 5), (17, 2), (18, 3)])
+def test_tc_radix32_fused_pair(lib_built, oracle, tmp_path, monkeypatch, prec, tol, logn, batch):
+    """The split form's pass pair on 32-sample tiles: each radix-2^7..2^9 pass
+    runs one radix-32 tensor-core stage (64 x 64 G, FP16 or BF16 hi/lo) and
+    an FP32 remainder.  Forced through the tuning cache, out of place on the
+    device (one launch a transform); FP64 gate in both directions, and
+    agreement with the 16-sample pair."""
+    torch = pytest.importorskip("torch")
+    import json
+    import gbfft
+    from gbfft import signals
+    n = 1 << logn
+    x = signals.tones_c64(batch, n, seed=1200 + logn)
+    outs = {}
+    for loge in (4, 5):
+        cache = tmp_path / f"tune_{prec}_{loge}.jsonl"
+        cache.write_text("\n".join(json.dumps({
+            "arch": "sm_103", "logn": logn, "precision": prec, "direction": d, "batch_log2": batch.bit_length() - 1,
+            "max_logr": 9, "persistent": 0, "fused": 1, "tile": 0, "loge": loge, "seconds": 1.0})
+            for d in (gbfft.FORWARD, gbfft.INVERSE)) + "\n")
+        monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+        outs[loge] = []
+        with gbfft.Context(0) as ctx:
+            ctx.set_precision(prec)
+            for direction in (gbfft.FORWARD, gbfft.INVERSE):
+                dx = torch.from_numpy(x).cuda()
+                dy = torch.full_like(dx, float("nan"))
+                l0 = ctx.launch_count()
+                ctx.c2c_device(dx, dy, n, batch, direction)
+                ctx.c2c_device(dx, dy, n, batch, direction)
+                torch.cuda.synchronize()
+                assert ctx.launch_count() - l0 == 2
+                outs[loge].append(dy.cpu().numpy())
+    for y, inv in zip(outs[5], (False, True)):
+        err = oracle.rel_l2(y, oracle.fft64(x, inverse=inv))
+        assert err <= tol, (inv, err)
+    for a, b in zip(outs[4], outs[5]):
+        assert oracle.rel_l2(b, a) <= 2 * tol

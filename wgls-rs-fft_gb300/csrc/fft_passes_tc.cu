@@ -41,12 +41,12 @@ constexpr int tc_groups() {
 // tile + column twiddles; the hi/lo A operands alias it while a tensor-core
 // DFT runs -- every tc_dft16 waits for the tile's readers before writing A),
 // then the two G parts, then the mbarrier, TMEM address and abort flag.
-template <int KIND, int THREADS, size_t TILE_BYTES>
+template <int KIND, int THREADS, size_t TILE_BYTES, int RADIX = 16>
 struct TcSmem {
-    using Gm = TcGeom<KIND>;
+    using Gm = TcGeom<KIND, RADIX>;
     static constexpr int NMMA = THREADS / 128;
     static_assert(THREADS % 128 == 0, "one M = 128 MMA per 128 threads");
-    static constexpr uint32_t TMEM_COLS = tc_tmem_cols(NMMA);
+    static constexpr uint32_t TMEM_COLS = tc_tmem_cols(NMMA * RADIX / 16);  // 2 RADIX columns per block
     static constexpr size_t A_BYTES = (size_t)THREADS * Gm::ROW_BYTES;
     static constexpr size_t REGION = ((2 * A_BYTES > TILE_BYTES ? 2 * A_BYTES : TILE_BYTES) + 1023) & ~(size_t)1023;
     static constexpr size_t OFF_G = REGION;
@@ -60,7 +60,7 @@ struct TcSmem {
 template <int KIND, class L>
 __device__ __forceinline__ void tc_cta_setup(uint8_t *smem, const uint4 *__restrict__ gtab, uint32_t *err,
                                              TcState &st) {
-    using Gm = TcGeom<KIND>;
+    using Gm = typename L::Gm;
     uint64_t *bar = (uint64_t *)(smem + L::OFF_MISC);
     uint32_t *s_taddr = (uint32_t *)(smem + L::OFF_MISC + 8);
     int *s_abort = (int *)(smem + L::OFF_MISC + 12);
@@ -158,21 +158,26 @@ fft_pass_tc_kernel(const float2 *in, float2 *out, int logn, int logp, const floa
 // both passes of a two-pass transform in one persistent launch
 // ---------------------------------------------------------------------------
 
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int KIND>
+// LE = 5: 32-sample tiles whose radix-32 sub-passes run on the tensor cores
+// (radix-32 G, 64 TMEM columns per 128 threads); 16-bit kinds only.
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int KIND, int LE = 4>
 struct FusedTcCfg {
-    using F = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, 0>;
-    using L = TcSmem<KIND, THREADS, F::SMEM>;
+    using F = FusedCfg<LOGRA, LOGRB, THREADS, LOGN, 0, LE>;
+    using L = TcSmem<KIND, THREADS, F::SMEM, LE == 5 ? 32 : 16>;
     static constexpr int MINB = L::FIT < F::MINB ? (L::FIT < 1 ? 1 : L::FIT) : F::MINB;
 };
 
-template <int LOGRA, int LOGRB, int THREADS, int LOGN, int KIND>
-__global__ void __launch_bounds__(THREADS, (FusedTcCfg<LOGRA, LOGRB, THREADS, LOGN, KIND>::MINB))
+template <int LOGRA, int LOGRB, int THREADS, int LOGN, int KIND, int LE = 4>
+__global__ void __launch_bounds__(THREADS, (FusedTcCfg<LOGRA, LOGRB, THREADS, LOGN, KIND, LE>::MINB))
 fft_fused_tc_kernel(FusedParams P) {
-    using C = FusedTcCfg<LOGRA, LOGRB, THREADS, LOGN, KIND>;
+    using C = FusedTcCfg<LOGRA, LOGRB, THREADS, LOGN, KIND, LE>;
     extern __shared__ __align__(1024) uint8_t smem_ftc[];
     TcState st;
     tc_cta_setup<KIND, typename C::L>(smem_ftc, P.gtab, P.err, st);
-    fused_loop<LOGRA, LOGRB, THREADS, LOGN, 0>(P, (float2 *)smem_ftc, DftTc<KIND>{&st});
+    if constexpr (LE == 5)
+        fused_loop<LOGRA, LOGRB, THREADS, LOGN, 0, 5>(P, (float2 *)smem_ftc, DftTc32<KIND>{&st});
+    else
+        fused_loop<LOGRA, LOGRB, THREADS, LOGN, 0>(P, (float2 *)smem_ftc, DftTc<KIND>{&st});
     fused_finish<THREADS>(P);
     tc_cta_teardown<typename C::L>(st);
 }
@@ -229,12 +234,13 @@ cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uin
     return cudaLaunchKernel(d.fn, dim3((unsigned)tiles), dim3(d.threads), args, d.smem, stream);
 }
 
-template <int LOGRA, int LOGRB, int THREADS, int KIND>
+template <int LOGRA, int LOGRB, int THREADS, int KIND, int LE = 4>
 static void fused_tc_describe(FusedDesc &d) {
     constexpr int LOGN = LOGRA + LOGRB;
-    using C = FusedTcCfg<LOGRA, LOGRB, THREADS, LOGN, KIND>;
+    using C = FusedTcCfg<LOGRA, LOGRB, THREADS, LOGN, KIND, LE>;
     using F = typename C::F;
-    d.fn = (const void *)fft_fused_tc_kernel<LOGRA, LOGRB, THREADS, LOGN, KIND>;
+    d.fn = (const void *)fft_fused_tc_kernel<LOGRA, LOGRB, THREADS, LOGN, KIND, LE>;
+    d.loge = LE;
     d.threads = THREADS;
     d.smem = C::L::SMEM;
     d.logra = LOGRA;
@@ -248,7 +254,22 @@ static void fused_tc_describe(FusedDesc &d) {
 }
 
 template <int KIND>
-static bool fused_tc_info_kind(int logr1, int logr2, FusedDesc &d) {
+static bool fused_tc_info_kind(int logr1, int logr2, FusedDesc &d, int loge) {
+    if (loge == 5) {
+        if constexpr (KIND == kTcTF32) {
+            return false;
+        } else {
+#define GBFFT_FTC5(A, B) \
+    if (logr1 == A && logr2 == B) { fused_tc_describe<A, B, 256, KIND, 5>(d); return true; }
+            GBFFT_FTC5(8, 7)
+            GBFFT_FTC5(8, 8)
+            GBFFT_FTC5(9, 8)
+            GBFFT_FTC5(9, 9)
+#undef GBFFT_FTC5
+            return false;
+        }
+    }
+    if (loge != 4) return false;
 #define GBFFT_FTC(A, B, T) \
     if (logr1 == A && logr2 == B) { fused_tc_describe<A, B, T, KIND>(d); return true; }
     GBFFT_FTC(8, 7, 256)
@@ -259,11 +280,11 @@ static bool fused_tc_info_kind(int logr1, int logr2, FusedDesc &d) {
     return false;
 }
 
-bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d) {
+bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d, int loge) {
     switch (tc_kind_of_precision(precision)) {
-        case kTcBF16: return fused_tc_info_kind<kTcBF16>(logr1, logr2, d);
-        case kTcTF32: return fused_tc_info_kind<kTcTF32>(logr1, logr2, d);
-        default: return fused_tc_info_kind<kTcF16>(logr1, logr2, d);
+        case kTcBF16: return fused_tc_info_kind<kTcBF16>(logr1, logr2, d, loge);
+        case kTcTF32: return fused_tc_info_kind<kTcTF32>(logr1, logr2, d, loge);
+        default: return fused_tc_info_kind<kTcF16>(logr1, logr2, d, loge);
     }
 }
 
@@ -300,8 +321,34 @@ __global__ void tc_gtab_kernel(uint8_t *out) {
     *(uint32_t *)(out + 8192 + 4096 + off32) = tl;
 }
 
+// Radix-32 G (64 x 64) parts for the 32-sample tiles, after the radix-16 ones:
+// [fp16 hi | fp16 lo | bf16 hi | bf16 lo], 8192 bytes each, from byte 16384.
+__global__ void tc_gtab32_kernel(uint8_t *out) {
+    const int i = threadIdx.x + blockIdx.x * blockDim.x;
+    if (i >= 64 * 64) return;
+    const int n = i / 64, k = i % 64;  // operand B is K-major: row n (output column), element k
+    const int q = n & 31, e = k & 31;
+    double sn, cs;
+    sincospi(2.0 * (double)((q * e) & 31) / 32.0, &sn, &cs);
+    double g;
+    if (n < 32) g = (k < 32) ? cs : sn;
+    else g = (k < 32) ? -sn : cs;
+    const float gf = (float)g;
+    const uint32_t off = TcGeom<kTcF16, 32>::elem_offset(n, k);
+    const __half h = __float2half_rn(gf);
+    const __half l = __float2half_rn(gf - __half2float(h));
+    const __nv_bfloat16 bh = __float2bfloat16_rn(gf);
+    const __nv_bfloat16 bl = __float2bfloat16_rn(gf - __bfloat162float(bh));
+    uint8_t *base = out + TcGeom<kTcF16, 32>::GTAB_OFF;
+    *(uint16_t *)(base + 0 * 8192 + off) = __half_as_ushort(h);
+    *(uint16_t *)(base + 1 * 8192 + off) = __half_as_ushort(l);
+    *(uint16_t *)(base + 2 * 8192 + off) = __bfloat16_as_ushort(bh);
+    *(uint16_t *)(base + 3 * 8192 + off) = __bfloat16_as_ushort(bl);
+}
+
 cudaError_t tc_gtab_fill(void *out, cudaStream_t stream) {
     tc_gtab_kernel<<<4, 256, 0, stream>>>((uint8_t *)out);
+    tc_gtab32_kernel<<<16, 256, 0, stream>>>((uint8_t *)out);
     return cudaGetLastError();
 }
 

@@ -43,22 +43,27 @@ enum : int { kTcF16 = 0, kTcBF16 = 1, kTcTF32 = 2 };
 
 constexpr uint32_t kTcLbo = 128;  // bytes between K-adjacent core matrices
 
-// Geometry of one operand kind: 32 values per operand row.
-template <int KIND>
+// Geometry of one operand kind for RADIX-point DFTs: 2 RADIX values per
+// operand row (Re | Im), a (2 RADIX) x (2 RADIX) G.  RADIX 16 for every kind;
+// RADIX 32 (the 32-sample tiles) for the 16-bit kinds.
+template <int KIND, int RADIX = 16>
 struct TcGeom {
+    static_assert(RADIX == 16 || (RADIX == 32 && KIND != kTcTF32), "radix-32 operands are 16-bit");
+    static constexpr int VALS = 2 * RADIX;                 // values per row
     static constexpr int ELEM = KIND == kTcTF32 ? 4 : 2;  // bytes per value
-    static constexpr int ROW_BYTES = 32 * ELEM;            // one A row
+    static constexpr int ROW_BYTES = VALS * ELEM;          // one A row
     static constexpr int KB = ROW_BYTES / 16;              // K-blocks (core matrices) per row block
     static constexpr uint32_t SBO = KB * 128u;             // bytes between row-adjacent core matrices
-    static constexpr int G_BYTES = 32 * ROW_BYTES;         // one 32 x 32 G part (hi or lo)
+    static constexpr int G_BYTES = VALS * ROW_BYTES;       // one G part (hi or lo)
     static constexpr int NKSTEP = ROW_BYTES / 32;          // MMAs along K (32 bytes of K each)
     // byte offset of the kind's [hi | lo] parts in the G table
-    static constexpr int GTAB_OFF = KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 4096 : 8192);
+    static constexpr int GTAB_OFF = RADIX == 32 ? (KIND == kTcF16 ? 16384 : 32768)
+                                                : (KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 4096 : 8192));
     // Instruction descriptor: D F32, A/B F16 (0) / BF16 (1) under kind::f16 or
-    // TF32 (2) under kind::tf32, both K-major, M = 128, N = 32.
+    // TF32 (2) under kind::tf32, both K-major, M = 128, N = 2 RADIX.
     static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 1 : 2)) << 7) |
                                       ((uint32_t)(KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 1 : 2)) << 10) |
-                                      ((32u >> 3) << 17) | ((128u >> 4) << 24);
+                                      (((uint32_t)VALS >> 3) << 17) | ((128u >> 4) << 24);
     // Byte offset of value (row, k) of a K-major no-swizzle operand.
     __host__ __device__ static constexpr uint32_t elem_offset(uint32_t row, uint32_t k) {
         return ((row >> 3) * KB + ((k * ELEM) >> 4)) * 128u + (row & 7) * 16u + ((k * ELEM) & 15u);
@@ -197,11 +202,14 @@ struct TcState {
     uint32_t spin_limit;
 };
 
-// Forward 16-point DFT of x (natural order in, natural order out) on the
-// tensor cores.  Must be called by all threads of the CTA at the same point.
-template <int KIND>
-__device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
-    using Gm = TcGeom<KIND>;
+// Forward RADIX-point DFT of x (natural order in, natural order out) on the
+// tensor cores, RADIX = 16 or 32 (32: 16-bit kinds, the 32-sample tiles; the
+// state's G parts must then be the radix-32 ones).  Must be called by all
+// threads of the CTA at the same point.
+template <int KIND, int RADIX>
+__device__ __forceinline__ void tc_dft(float2 (&x)[RADIX], TcState &s) {
+    using Gm = TcGeom<KIND, RADIX>;
+    constexpr int V = Gm::VALS;
     const uint32_t r = threadIdx.x;
     float up = 1.f;
     if constexpr (KIND == kTcTF32) {
@@ -209,12 +217,12 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
         // have finished reading its exchange inputs before any thread writes A.
         __syncthreads();
 #pragma unroll
-        for (int kb = 0; kb < 8; ++kb) {  // 8 chunks of 4 K-values (16 bytes)
+        for (int kb = 0; kb < V / 4; ++kb) {  // chunks of 4 K-values (16 bytes)
             uint32_t h[4], l[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const int k = 4 * kb + i;
-                tc_split_tf32(k < 16 ? x[k].x : x[k - 16].y, h[i], l[i]);
+                tc_split_tf32(k < RADIX ? x[k].x : x[k - RADIX].y, h[i], l[i]);
             }
             const uint32_t off = Gm::elem_offset(r, 4 * kb);
             *(uint4 *)(s.a_hi + off) = make_uint4(h[0], h[1], h[2], h[3]);
@@ -225,7 +233,7 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
         // 1. exact power-of-two scaling: largest |component| to [1, 2)
         float m = 0.f;
 #pragma unroll
-        for (int e = 0; e < 16; ++e) m = fmaxf(m, fmaxf(fabsf(x[e].x), fabsf(x[e].y)));
+        for (int e = 0; e < RADIX; ++e) m = fmaxf(m, fmaxf(fabsf(x[e].x), fabsf(x[e].y)));
         int ex = 0;
         if (m > 0.f) {
             ex = (int)((__float_as_uint(m) >> 23) & 0xff) - 127;
@@ -236,18 +244,21 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
         up = __uint_as_float((uint32_t)(127 + ex) << 23);                // 2^ex
         // A shares its bytes with the FP32 exchange tile (see above).
         __syncthreads();
-        // 2. split into hi/lo rows of A
-        uint32_t hi[16], lo[16];
+        // 2. split into hi/lo rows of A, 8 K-values (16 bytes) at a time:
+        //    K-values 0..RADIX-1 are Re x, RADIX..2 RADIX-1 are Im x
 #pragma unroll
-        for (int e = 0; e < 16; e += 2) {
-            tc_split2<BF16>(x[e].x * down, x[e + 1].x * down, hi[e / 2], lo[e / 2]);
-            tc_split2<BF16>(x[e].y * down, x[e + 1].y * down, hi[8 + e / 2], lo[8 + e / 2]);
-        }
+        for (int kb = 0; kb < V / 8; ++kb) {
+            uint32_t hi[4], lo[4];
 #pragma unroll
-        for (int kb = 0; kb < 4; ++kb) {  // 4 chunks of 8 K-values (16 bytes)
-            const uint32_t off = Gm::elem_offset(r, kb * 8);
-            *(uint4 *)(s.a_hi + off) = make_uint4(hi[4 * kb], hi[4 * kb + 1], hi[4 * kb + 2], hi[4 * kb + 3]);
-            *(uint4 *)(s.a_lo + off) = make_uint4(lo[4 * kb], lo[4 * kb + 1], lo[4 * kb + 2], lo[4 * kb + 3]);
+            for (int i = 0; i < 4; ++i) {
+                const int k = 8 * kb + 2 * i;
+                const float2 a = x[k % RADIX], b = x[(k + 1) % RADIX];
+                if (k < RADIX) tc_split2<BF16>(a.x * down, b.x * down, hi[i], lo[i]);
+                else tc_split2<BF16>(a.y * down, b.y * down, hi[i], lo[i]);
+            }
+            const uint32_t off = Gm::elem_offset(r, 8 * kb);
+            *(uint4 *)(s.a_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+            *(uint4 *)(s.a_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
         }
     }
     fence_proxy_async_smem();  // generic-proxy writes -> visible to the tensor core
@@ -262,7 +273,7 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
             const uint32_t ah = smem_u32(s.a_hi), al = smem_u32(s.a_lo);
             const uint32_t gh = smem_u32(s.g_hi), gl = smem_u32(s.g_lo);
             for (uint32_t mb = 0; mb < s.nmma; ++mb) {
-                const uint32_t d = s.taddr + mb * 32;
+                const uint32_t d = s.taddr + mb * V;
                 const uint32_t arow = mb * 128 * Gm::ROW_BYTES;  // 128 rows = 16 row blocks
                 uint32_t acc = 0;
 #pragma unroll
@@ -290,20 +301,28 @@ __device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) {
     }
     __syncthreads();
     s.parity ^= 1u;
-    // 4. read this thread's row back: lanes of warp (r / 32) % 4, columns of block r / 128
+    // 4. read this thread's row back: lanes of warp (r / 32) % 4, columns of
+    //    block r / 128; 32 columns at a time (Re X, then Im X for RADIX 32)
     tc_fence_after();
+    const uint32_t taddr = s.taddr + ((((r >> 5) & 3) * 32) << 16) + (r >> 7) * V;
     uint32_t d[32];
-    const uint32_t taddr = s.taddr + ((((r >> 5) & 3) * 32) << 16) + (r >> 7) * 32;
-    tmem_ld32(taddr, d);
-    tc_fence_before();
-    if constexpr (KIND == kTcTF32) {
-#pragma unroll
-        for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]), __uint_as_float(d[16 + q]));
-    } else {
+    if constexpr (RADIX == 16) {
+        tmem_ld32(taddr, d);
 #pragma unroll
         for (int q = 0; q < 16; ++q) x[q] = make_float2(__uint_as_float(d[q]) * up, __uint_as_float(d[16 + q]) * up);
+    } else {
+        tmem_ld32(taddr, d);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) x[q].x = __uint_as_float(d[q]) * up;
+        tmem_ld32(taddr + 32, d);
+#pragma unroll
+        for (int q = 0; q < 32; ++q) x[q].y = __uint_as_float(d[q]) * up;
     }
+    tc_fence_before();
 }
+
+template <int KIND>
+__device__ __forceinline__ void tc_dft16(float2 (&x)[16], TcState &s) { tc_dft<KIND, 16>(x, s); }
 
 // Butterfly engine for pass_tile / rows_tile: radix-16 butterflies on the
 // tensor cores, the radix 2/4/8 remainder on the FP32 pipes.
@@ -313,6 +332,19 @@ struct DftTc {
     template <int R>
     __device__ __forceinline__ void run(float2 (&x)[R]) {
         if constexpr (R == 16) tc_dft16<KIND>(x, *s);
+        else Dft<R>::run(x);
+    }
+};
+
+// Engine for the 32-sample tiles (16-bit kinds): radix-32 butterflies on the
+// tensor cores (one per thread, so one operand row per thread), every smaller
+// radix on the FP32 pipes.
+template <int KIND>
+struct DftTc32 {
+    TcState *s;
+    template <int R>
+    __device__ __forceinline__ void run(float2 (&x)[R]) {
+        if constexpr (R == 32) tc_dft<KIND, 32>(x, *s);
         else Dft<R>::run(x);
     }
 };

@@ -126,9 +126,12 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         // the pair with 32 samples a thread (radix-32 sub-passes) first where a
         // pass has radix 2^9 or more: measured faster at 2^17..2^20 (177 / 178.5 /
         // 150.7 / 155.9 against 174.7 / 166.2 / 145.6 / 144.7 GSa/s); after the
-        // 16-sample pair otherwise
-        const bool e32 = !tc && parts.size() == 2 && fused2_kernel_info(parts[0], parts[1], fd, 5);
-        const bool e32_first = e32 && parts[0] >= 9;
+        // 16-sample pair otherwise.  The split form's 32-sample pair (one radix-32
+        // tensor-core stage a pass) runs 2 CTAs per SM against 4 and measured
+        // slower at 2^16 (FP16 135.6 vs 142.3 GSa/s): a candidate only
+        const bool e32 = parts.size() == 2 && (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, fd, 5)
+                                                  : fused2_kernel_info(parts[0], parts[1], fd, 5));
+        const bool e32_first = e32 && !tc && parts[0] >= 9;
         if (e32_first) c.push_back(PlanVariant{m, false, true, 0, 5});
         if (parts.size() == 2 && (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, fd)
                                      : fused2_kernel_info(parts[0], parts[1], fd)))
@@ -212,7 +215,7 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         }
         p.tw_entries = multipass_segments(logn, p.passes, 0, segs, p.tw_lo_offset, p.tw_hi_offset, p.tw_split);
         if (fused3 || (v.fused && parts.size() == 2 &&
-                       (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, p.fused)
+                       (tc ? fused_tc_kernel_info(parts[0], parts[1], precision, p.fused, v.loge)
                            : fused2_kernel_info(parts[0], parts[1], p.fused, v.loge)))) {
             if (p.fused.loge != 4) {
                 // the pair's tiles follow their own sub-pass schedule: append its tables

@@ -116,7 +116,8 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
 // fft_passes_tc.cu (split-precision tensor-core form)
 bool pass_tc_kernel_info(int logr, bool first, int precision, PassDesc &d);
 // both passes of a two-pass transform in one persistent launch (radices 2^8/2^7 .. 2^9/2^9)
-bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d);
+// loge 5: 32-sample tiles with radix-32 tensor-core sub-DFTs (16-bit kinds)
+bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d, int loge = 4);
 cudaError_t pass_tc_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                            const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, const void *gtab,
@@ -129,8 +130,9 @@ cudaError_t rows_tc_prepare(RowsKernelInfo &k);
 cudaError_t rows_tc_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
                            const float2 *tw, int direction, int logn, const void *gtab, uint32_t *err,
                            cudaStream_t stream, LoadOps ops);
-// G table: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (2 KB each), [TF32 hi | TF32 lo] (4 KB each)
-constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096;
+// G table: radix 16: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (2 KB each), [TF32 hi | TF32 lo]
+// (4 KB each); radix 32: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (8 KB each)
+constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096 + 4 * 8192;
 
 // fft_fused2.cu, fft_fused3.cu
 // loge 5: tiles of 32 samples a thread (radix-32 sub-passes), pairs with a radix-2^9/2^10 pass

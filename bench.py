@@ -55,6 +55,7 @@ WORKLOADS = {
     "n1048576_b64": (20, 64, "normal", 2),
     "n4194304_b64": (22, 64, "normal", 3),
     "n16777216_b4": (24, 4, "normal", 3),
+    "n33554432_b2": (25, 2, "normal", 3),
     "n67108864_b1": (26, 1, "normal", 3),
 }
 DEFAULT_WORKLOAD = "n4096_b16384"

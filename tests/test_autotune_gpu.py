@@ -175,6 +175,37 @@ def test_three_pass_first_pass_32_samples(tmp_path, monkeypatch, oracle, lib_bui
         assert oracle.rel_l2(outs[5][0], ref) <= TOL_REL_L2
 
 
+@pytest.mark.parametrize("logn,batch,loge,persistent", [
+    (25, 2, 5, 0), (25, 2, 4, 0), (26, 1, 5, 0), (26, 1, 4, 0), (25, 1, 5, 1)])
+def test_three_pass_first_pass_8_columns(tmp_path, monkeypatch, oracle, lib_built, logn, batch, loge, persistent):
+    """N = 2^25 / 2^26 as (L-16, 8, 8) with the radix-2^9 / 2^10 first pass on
+    8 columns a CTA (plan tile 3; two CTAs per SM) instead of 16.  Each column's
+    arithmetic is unchanged, so both directions give the same bits as the
+    16-column first pass; 2^25 also meets the FP64 gate."""
+    import numpy as np
+
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=1300 + logn + loge)
+    outs = {}
+    for tile in (0, 3):
+        cache = tmp_path / f"tune_{tile}.jsonl"
+        lines = []
+        for d in (gbfft.FORWARD, gbfft.INVERSE):
+            line = json.loads(_cache_line(logn, batch, d, 10, persistent, tile=tile, loge=loge))
+            line["fused"] = 1
+            lines.append(json.dumps(line))
+        cache.write_text("\n".join(lines) + "\n")
+        monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+        with gbfft.Context(0) as ctx:
+            outs[tile] = [ctx.c2c_host(x, d) for d in (gbfft.FORWARD, gbfft.INVERSE)]
+    for a, b in zip(outs[0], outs[3]):
+        assert np.array_equal(a, b)
+    if logn == 25 and persistent == 0:
+        ref = np.fft.fft(x.astype(np.complex128), axis=1)
+        assert oracle.rel_l2(outs[3][0], ref) <= TOL_REL_L2
+
+
 @pytest.mark.parametrize("logn,batch,loge", [(21, 3, 4), (22, 2, 4), (25, 1, 5)])
 def test_three_pass_persistent_first_pass(tmp_path, monkeypatch, oracle, lib_built, logn, batch, loge):
     """Three-pass plans whose lone first pass runs as a persistent tile loop

@@ -11,7 +11,9 @@
 // One CTA takes 16 adjacent columns of one transform: lanes are mapped column
 // fastest, so every global load and store moves 16 x 8 = 128 contiguous bytes
 // per half-warp, and the shared-memory tile [row][16 columns] is free of bank
-// conflicts for every access pattern.  The first pass (p = 1) writes each
+// conflicts for every access pattern.  First passes of radix 2^9 / 2^10 may
+// take 8 columns instead (CL = 3: 64-byte row segments, half the tile, two
+// CTAs per SM where 16 columns fit one).  The first pass (p = 1) writes each
 // column's R outputs contiguously; it stages them through shared memory
 // (XOR-swizzled [column][row]) so that its HBM stores are fully coalesced too.
 //
@@ -30,29 +32,30 @@ namespace gbfft {
 
 // LE: log2 of the samples a thread holds (4: 64 registers; 5: radix-32
 // sub-passes at 128 registers, one exchange fewer for radix 2^9 / 2^10).
-template <int LOGR, int LE = 4>
-struct PassCfg : PassTileCfg<LOGR, 1, LE> {
-    using K = PassTileCfg<LOGR, 1, LE>;
+// CL: log2 of the columns a CTA takes.
+template <int LOGR, int LE = 4, int CL = kColsLog>
+struct PassCfg : PassTileCfg<LOGR, 1, LE, CL> {
+    using K = PassTileCfg<LOGR, 1, LE, CL>;
     static constexpr int REGS = LE == 4 ? 64 : 128;
     static constexpr int MINB = K::THREADS * REGS >= 65536 ? 1 : 65536 / (K::THREADS * REGS);
     static constexpr size_t SMEM = K::SMEM_ELEMS * sizeof(float2);
 };
 
-template <int LOGR, bool FIRST, int LE = 4>
-__global__ void __launch_bounds__(PassCfg<LOGR, LE>::THREADS, PassCfg<LOGR, LE>::MINB)
+template <int LOGR, bool FIRST, int LE = 4, int CL = kColsLog>
+__global__ void __launch_bounds__(PassCfg<LOGR, LE, CL>::THREADS, PassCfg<LOGR, LE, CL>::MINB)
 fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                 const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                 float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
     extern __shared__ float2 smem_pass[];
     const int lognc = logn - LOGR;                     // log2 (columns per transform)
     const uint64_t tile = blockIdx.x;
-    const uint64_t b = tile >> (lognc - kColsLog);
+    const uint64_t b = tile >> (lognc - CL);
     PassArgs a;
     a.src = in + (b << logn);
     a.dst = out + (b << logn);
     a.logn = logn;
     a.logp = logp;
-    a.col0 = (uint32_t)(tile & ((1ull << (lognc - kColsLog)) - 1)) << kColsLog;
+    a.col0 = (uint32_t)(tile & ((1ull << (lognc - CL)) - 1)) << CL;
     a.tw_sub = tw;
     a.tw_lo = tw_lo;
     a.tw_hi = tw_hi;
@@ -63,14 +66,14 @@ fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 
     a.coherent_load = false;
     a.row = (uint32_t)b;
     a.ops = ops;
-    pass_tile<LOGR, 1, FIRST, DftRegs, 0, -1, LE>(a, smem_pass);
+    pass_tile<LOGR, 1, FIRST, DftRegs, 0, -1, LE, CL>(a, smem_pass);
 }
 
 // Persistent variant: each CTA walks tiles blockIdx.x, +gridDim.x, ... and asks
-// L2 for the next tile's R row segments (128 bytes each, one per thread)
+// L2 for the next tile's R row segments (2^CL x 8 bytes each, one per thread)
 // before computing the current one.
-template <int LOGR, bool FIRST, int LE = 4>
-__global__ void __launch_bounds__(PassCfg<LOGR, LE>::THREADS, PassCfg<LOGR, LE>::MINB)
+template <int LOGR, bool FIRST, int LE = 4, int CL = kColsLog>
+__global__ void __launch_bounds__(PassCfg<LOGR, LE, CL>::THREADS, PassCfg<LOGR, LE, CL>::MINB)
 fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                            const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops,
@@ -78,12 +81,12 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
     extern __shared__ float2 smem_pass[];
     constexpr int R = 1 << LOGR;
     const int lognc = logn - LOGR;
-    const uint64_t tiles_per_row = 1ull << (lognc - kColsLog);
+    const uint64_t tiles_per_row = 1ull << (lognc - CL);
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const uint64_t next = tile + gridDim.x;
         if (next < ntiles) {
-            const float2 *nb = in + ((next / tiles_per_row) << logn) + ((next % tiles_per_row) << kColsLog);
-            for (int m = threadIdx.x; m < R; m += PassCfg<LOGR, LE>::THREADS) prefetch_l2(nb + ((uint64_t)m << lognc));
+            const float2 *nb = in + ((next / tiles_per_row) << logn) + ((next % tiles_per_row) << CL);
+            for (int m = threadIdx.x; m < R; m += PassCfg<LOGR, LE, CL>::THREADS) prefetch_l2(nb + ((uint64_t)m << lognc));
         }
         const uint64_t b = tile / tiles_per_row;
         PassArgs a;
@@ -91,7 +94,7 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
         a.dst = out + (b << logn);
         a.logn = logn;
         a.logp = logp;
-        a.col0 = (uint32_t)((tile % tiles_per_row) << kColsLog);
+        a.col0 = (uint32_t)((tile % tiles_per_row) << CL);
         a.tw_sub = tw;
         a.tw_lo = tw_lo;
         a.tw_hi = tw_hi;
@@ -102,7 +105,7 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
         a.coherent_load = false;
         a.row = (uint32_t)b;
         a.ops = ops;
-        pass_tile<LOGR, 1, FIRST, DftRegs, 0, -1, LE>(a, smem_pass);
+        pass_tile<LOGR, 1, FIRST, DftRegs, 0, -1, LE, CL>(a, smem_pass);
         __syncthreads();  // shared memory is reused by the next tile
     }
 }
@@ -119,13 +122,37 @@ static void pass_describe(PassDesc &d, bool first) {
                             : (const void *)fft_pass_persistent_kernel<LOGR, false, LE>;
     d.threads = C::THREADS;
     d.smem = C::SMEM;
-    d.cols = kCols;
+    d.cols = C::COLS;
     d.nseg = subcfg_segments<LOGR, LE>(d.segs, 0);
     d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
 }
 
-bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge) {
+// First pass of 8 columns a CTA.
+template <int LOGR, int LE>
+static void pass_describe_first8(PassDesc &d) {
+    using C = PassCfg<LOGR, LE, 3>;
+    d.fn = (const void *)fft_pass_kernel<LOGR, true, LE, 3>;
+    d.fn_persistent = (const void *)fft_pass_persistent_kernel<LOGR, true, LE, 3>;
+    d.threads = C::THREADS;
+    d.smem = C::SMEM;
+    d.cols = C::COLS;
+    d.nseg = subcfg_segments<LOGR, LE>(d.segs, 0);
+    d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
+}
+
+bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge, int cols_log) {
     d.logr = logr;
+    if (cols_log == 3) {  // first passes of radix 2^9 / 2^10 only
+        if (!first) return false;
+        switch (logr * 10 + loge) {
+            case 94: pass_describe_first8<9, 4>(d); return true;
+            case 95: pass_describe_first8<9, 5>(d); return true;
+            case 104: pass_describe_first8<10, 4>(d); return true;
+            case 105: pass_describe_first8<10, 5>(d); return true;
+            default: return false;
+        }
+    }
+    if (cols_log != kColsLog) return false;
     if (loge == 5) {  // first passes of radix 2^9 / 2^10 (N = 2^25, 2^26 as (L-16, 8, 8))
         if (!first) return false;
         switch (logr) {
@@ -161,7 +188,7 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                         float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
                         bool persistent, int sms, LoadOps ops) {
-    uint64_t tiles = batch << (logn - d.logr - kColsLog);
+    uint64_t tiles = (batch << (logn - d.logr)) / (uint64_t)d.cols;
     if (tiles == 0) return cudaSuccess;
     int logp = d.logp;
     if (persistent && d.fn_persistent && d.persist_ctas_per_sm > 0 && sms > 0) {

@@ -4,9 +4,9 @@
 //   rows_tile<LOGN, G>  -- G whole transforms of length 2^LOGN, one HBM read and
 //                          one HBM write per sample (the single-pass form).
 //   pass_tile<LOGR, NG, FIRST>
-//                       -- NG groups of 16 adjacent columns of one global
-//                          Stockham pass of radix R = 2^LOGR (multi-pass form).
-// Both use all G*T (resp. NG*16*T) threads of the CTA and __syncthreads().
+//                       -- NG groups of 16 (or 2^CL) adjacent columns of one
+//                          global Stockham pass of radix R = 2^LOGR (multi-pass form).
+// Both use all G*T (resp. NG*2^CL*T) threads of the CTA and __syncthreads().
 #pragma once
 #include "fft_smem.cuh"
 
@@ -120,7 +120,19 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
 
 // ---- global-pass tiles -----------------------------------------------------
 
-template <int LOGR, int I, int LE = 4, bool DONE = (I >= SubCfg<LOGR, LE>::NSUB)>
+// Row of the [row][2^CL column] exchange tile.  With 16 columns a warp spans
+// two rows, which fill the banks whatever their distance.  With 8 it spans four
+// (t = 4w .. 4w+3); after a sub-pass with p = 1 they are 2^PR apart and would
+// all share one half of the banks, so row bit 0 is flipped by row bit PR.  That
+// permutes every aligned group of four rows within itself, so the reads of rows
+// t + T e stay conflict-free.
+template <int CL, int PP, int PR>
+__device__ __forceinline__ int xrow(int row) {
+    if constexpr (CL < kColsLog && PP == 0) return row ^ ((row >> PR) & 1);
+    else return row;
+}
+
+template <int LOGR, int I, int LE = 4, int CL = kColsLog, bool DONE = (I >= SubCfg<LOGR, LE>::NSUB)>
 struct PassChain {
     using C = SubCfg<LOGR, LE>;
     template <class Eng>
@@ -132,16 +144,16 @@ struct PassChain {
         for (int b = 0; b < (C::E >> PR); ++b)
 #pragma unroll
             for (int q = 0; q < (1 << PR); ++q)
-                buf[(subpass_out_pos<PR, PP, C::LOGT>(t, b, q) << kColsLog) + c] = v[b + q * (C::E >> PR)];
+                buf[(xrow<CL, PP, PR>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q)) << CL) + c] = v[b + q * (C::E >> PR)];
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < C::E; ++e) v[e] = buf[((t + C::T * e) << kColsLog) + c];
+        for (int e = 0; e < C::E; ++e) v[e] = buf[(xrow<CL, PP, PR>(t + C::T * e) << CL) + c];
         subpass_run<LOGR, I, LE>(v, t, tw, eng);
-        PassChain<LOGR, I + 1, LE>::run(v, t, c, buf, tw, eng);
+        PassChain<LOGR, I + 1, LE, CL>::run(v, t, c, buf, tw, eng);
     }
 };
-template <int LOGR, int I, int LE>
-struct PassChain<LOGR, I, LE, true> {
+template <int LOGR, int I, int LE, int CL>
+struct PassChain<LOGR, I, LE, CL, true> {
     template <class Eng>
     __device__ __forceinline__ static void run(float2 (&)[SubCfg<LOGR, LE>::E], int, int, float2 *, const float2 *,
                                                Eng &) {}
@@ -152,12 +164,13 @@ __device__ __forceinline__ float2 twiddle_2level(const float2 *__restrict__ lo, 
     return cmul(ld_tw(hi + (ex >> split)), ld_tw(lo + (ex & ((1u << split) - 1))));
 }
 
-template <int LOGR, int NG, int LE = 4>
+template <int LOGR, int NG, int LE = 4, int CL = kColsLog>
 struct PassTileCfg {
     using S = SubCfg<LOGR, LE>;
-    static constexpr int THREADS = NG * kCols * S::T;
+    static constexpr int COLS = 1 << CL;
+    static constexpr int THREADS = NG * COLS * S::T;
     static constexpr int COLTW_STRIDE = S::E + 1;  // padded: conflict-free column reads
-    static constexpr size_t SMEM_ELEMS = (size_t)NG * kCols * S::N + (size_t)NG * kCols * COLTW_STRIDE;
+    static constexpr size_t SMEM_ELEMS = (size_t)NG * COLS * S::N + (size_t)NG * COLS * COLTW_STRIDE;
 };
 
 // Arguments of one global pass over one transform (offsets already applied).
@@ -165,7 +178,7 @@ struct PassArgs {
     const float2 *src;  // transform base, input of this pass
     float2 *dst;        // transform base, output of this pass
     int logn, logp;
-    uint32_t col0;      // first column of the tile (multiple of NG*16)
+    uint32_t col0;      // first column of the tile (multiple of NG * 2^CL)
     const float2 *tw_sub, *tw_lo, *tw_hi;
     int tw_split;
     float in_im;          // -1: conjugate the input (first pass of an inverse)
@@ -176,28 +189,32 @@ struct PassArgs {
     LoadOps ops;         // first pass: noise / window applied on load
 };
 
-// NG groups x 16 columns of one global Stockham pass of radix 2^LOGR.
+// NG groups x 2^CL columns (16 by default) of one global Stockham pass of radix 2^LOGR.
 // LOGN_CT / LOGP_CT: log2 N and log2 p when the caller knows them at compile
 // time (0 / -1: taken from a.logn / a.logp).  Constant sizes turn every
 // strided address and twiddle index into immediates.  LE: log2 of the
 // samples a thread holds (SubCfg; the sub-pass tables in a.tw_sub follow it).
-template <int LOGR, int NG, bool FIRST, class Eng = DftRegs, int LOGN_CT = 0, int LOGP_CT = -1, int LE = 4>
+// CL: log2 of the columns a group takes; 8 columns still move 64 contiguous
+// bytes per row and halve the tile, so a radix-2^9/2^10 tile fits twice per SM.
+template <int LOGR, int NG, bool FIRST, class Eng = DftRegs, int LOGN_CT = 0, int LOGP_CT = -1, int LE = 4,
+          int CL = kColsLog>
 __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng eng = Eng()) {
     using C = SubCfg<LOGR, LE>;
-    using K = PassTileCfg<LOGR, NG, LE>;
+    using K = PassTileCfg<LOGR, NG, LE, CL>;
     constexpr int R = C::N, T = C::T, E = C::E;
+    constexpr int COLS = 1 << CL;
     const int tid = threadIdx.x;
-    const int grp = tid / (kCols * T);
-    const int lt = tid - grp * (kCols * T);
-    const int c = lt & (kCols - 1);
-    const int t = lt >> kColsLog;
-    float2 *buf = smem + grp * (kCols * R);
-    float2 *coltw = smem + NG * kCols * R + grp * (kCols * K::COLTW_STRIDE);
+    const int grp = tid / (COLS * T);
+    const int lt = tid - grp * (COLS * T);
+    const int c = lt & (COLS - 1);
+    const int t = lt >> CL;
+    float2 *buf = smem + grp * (COLS * R);
+    float2 *coltw = smem + NG * COLS * R + grp * (COLS * K::COLTW_STRIDE);
     const int logn = LOGN_CT > 0 ? LOGN_CT : a.logn;
     const int logp = LOGP_CT >= 0 ? LOGP_CT : a.logp;
     const int tw_split = LOGN_CT > 0 ? (LOGN_CT + 1) / 2 : a.tw_split;
     const int lognc = logn - LOGR;
-    const uint32_t j0 = a.col0 + grp * kCols;
+    const uint32_t j0 = a.col0 + grp * COLS;
     const uint32_t j = j0 + c;
 
     float2 v[E];
@@ -232,7 +249,7 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
         const uint32_t pmask = (1u << logp) - 1;
         // per-column factors W_{E p}^{e k} = W_N^{(e k) << (logn - LOGE - logp)}
         const int sh_col = logn - C::LOGE - logp;
-        for (int i = lt; i < kCols * E; i += kCols * T) {
+        for (int i = lt; i < COLS * E; i += COLS * T) {
             const int cc = i >> C::LOGE, ee = i & (E - 1);
             const uint32_t kk = (j0 + cc) & pmask;
             coltw[cc * K::COLTW_STRIDE + ee] = twiddle_2level(a.tw_lo, a.tw_hi, (kk * ee) << sh_col, tw_split);
@@ -245,36 +262,38 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
         for (int e = 0; e < E; ++e) v[e] = cmul(v[e], cmul(w, coltw[c * K::COLTW_STRIDE + e]));
     }
     subpass_run<LOGR, 0, LE>(v, t, a.tw_sub, eng);
-    PassChain<LOGR, 1, LE>::run(v, t, c, buf, a.tw_sub, eng);
+    PassChain<LOGR, 1, LE, CL>::run(v, t, c, buf, a.tw_sub, eng);
 
     constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
     constexpr int NB = E >> LR;
     if (FIRST) {
         // Outputs of column j are contiguous at j R + q: stage them as
-        // [column][q ^ column] and store each group's 16 R-sample block linearly.
+        // [column][q ^ (column << (4 - CL))] (a warp's 32 / 2^CL rows of 2^CL
+        // columns then cover every bank pair twice) and store each group's
+        // 2^CL R-sample block linearly.
         __syncthreads();
 #pragma unroll
         for (int bb = 0; bb < NB; ++bb)
 #pragma unroll
             for (int q = 0; q < (1 << LR); ++q) {
                 const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
-                buf[c * R + (pos ^ c)] = v[bb + q * NB];
+                buf[c * R + (pos ^ (c << (kColsLog - CL)))] = v[bb + q * NB];
             }
         __syncthreads();
         float2 *blk = a.dst + (uint64_t)j0 * R;
         if (a.keep_l2) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const int lin = lt + kCols * T * e;
+                const int lin = lt + COLS * T * e;
                 const int cc = lin >> LOGR, q = lin & (R - 1);
-                __stcg(blk + lin, buf[cc * R + (q ^ cc)]);
+                __stcg(blk + lin, buf[cc * R + (q ^ (cc << (kColsLog - CL)))]);
             }
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
-                const int lin = lt + kCols * T * e;
+                const int lin = lt + COLS * T * e;
                 const int cc = lin >> LOGR, q = lin & (R - 1);
-                st_stream(blk + lin, buf[cc * R + (q ^ cc)]);
+                st_stream(blk + lin, buf[cc * R + (q ^ (cc << (kColsLog - CL)))]);
             }
         }
     } else {

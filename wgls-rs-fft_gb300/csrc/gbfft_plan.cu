@@ -110,13 +110,17 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
     if (!tc && fused3_kernel_info(logn, fd)) {
         // its first pass with 32 samples a thread where that exists (radix 2^9 /
         // 2^10: N = 2^25, 2^26), measured faster (2^26: 114.9 vs 112.9 GSa/s)
+        // and on 8 columns a CTA (two CTAs per SM instead of one; same bits):
+        // 2^26: 118.5 vs 115.9, 2^25: 131.0 vs 128.7 GSa/s
         PassDesc pd;
         const bool e32 = pass_kernel_info(logn - 16, true, pd, 5);
+        if (pass_kernel_info(logn - 16, true, pd, 5, 3)) c.push_back(PlanVariant{10, false, true, 3, 5});
         if (e32) c.push_back(PlanVariant{10, false, true, 0, 5});
         c.push_back(PlanVariant{10, false, true});
         // the lone first pass as a persistent tile loop with L2 prefetch of the next tile
         if (e32) c.push_back(PlanVariant{10, true, true, 0, 5});
         c.push_back(PlanVariant{10, true, true});
+        if (pass_kernel_info(logn - 16, true, pd, 4, 3)) c.push_back(PlanVariant{10, false, true, 3, 4});
     }
     for (int m = top; m >= 7; --m) {
         const std::vector<int> parts = split_passes(logn, m);
@@ -199,7 +203,8 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
         for (size_t i = 0; i < parts.size(); ++i) {
             PassDesc d;
             const bool ok = tc ? pass_tc_kernel_info(parts[i], i == 0, precision, d)
-                               : pass_kernel_info(parts[i], i == 0, d, (fused3 && i == 0) ? v.loge : 4);
+                               : pass_kernel_info(parts[i], i == 0, d, (fused3 && i == 0) ? v.loge : 4,
+                                                  (fused3 && i == 0 && v.tile) ? v.tile : 4);
             if (!ok) {
                 why = std::string("no ") + (tc ? "tensor-core " : "") + "pass kernel for radix 2^" +
                       std::to_string(parts[i]);

@@ -68,7 +68,8 @@ struct PlanVariant {
     int max_logr = 10;
     bool persistent = false;
     bool fused = false;
-    int tile = 0;  // single pass: log2 of the samples a CTA moves (0: 2^12), i.e. transforms per CTA
+    int tile = 0;  // single pass: log2 of the samples a CTA moves (0: 2^12), i.e. transforms per CTA;
+                   // three passes: log2 of the columns a first-pass CTA takes (0: 16)
     int loge = 4;  // single pass: log2 of the samples a thread holds (5: radix-32 sub-passes, N = 2^13, 2^14)
     bool operator<(const PlanVariant &o) const {
         if (max_logr != o.max_logr) return max_logr < o.max_logr;
@@ -106,7 +107,7 @@ struct Plan {
 
 // fft_passes.cu
 // loge 5: 32 samples a thread, for the first pass of radix 2^9 / 2^10 only
-bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge = 4);
+bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge = 4, int cols_log = 4);
 cudaError_t pass_prepare(PassDesc &d);
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,

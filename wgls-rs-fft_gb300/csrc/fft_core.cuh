@@ -211,6 +211,7 @@ __device__ __forceinline__ float2 pipeline_noise(uint32_t n, uint32_t row, uint3
 // Streaming global access: every sample is read once and written once.
 __device__ __forceinline__ float2 ld_stream(const float2 *p) { return __ldcs(p); }
 __device__ __forceinline__ void st_stream(float2 *p, float2 v) { __stcs(p, v); }
+__device__ __forceinline__ void st_stream(float4 *p, float4 v) { __stcs(p, v); }
 // Twiddles are shared by every transform of a plan: keep them cached.
 __device__ __forceinline__ float2 ld_tw(const float2 *p) { return __ldg(p); }
 // Bring one 128-byte line toward L2 ahead of its use (a hint: never faults on

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(PassCfg<LOGR, LE, CL>::THREADS, PassCfg<LOGR, 
 fft_pass_kernel(const float2 *in, float2 *out, int logn, int logp, const float2 *__restrict__ tw,
                 const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                 float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
-    extern __shared__ float2 smem_pass[];
+    extern __shared__ __align__(16) float2 smem_pass[];
     const int lognc = logn - LOGR;                     // log2 (columns per transform)
     const uint64_t tile = blockIdx.x;
     const uint64_t b = tile >> (lognc - CL);
@@ -78,7 +78,7 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
                            const float2 *__restrict__ tw_lo, const float2 *__restrict__ tw_hi, int tw_split,
                            float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops,
                            uint64_t ntiles) {
-    extern __shared__ float2 smem_pass[];
+    extern __shared__ __align__(16) float2 smem_pass[];
     constexpr int R = 1 << LOGR;
     const int lognc = logn - LOGR;
     const uint64_t tiles_per_row = 1ull << (lognc - CL);
@@ -190,6 +190,8 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
                         bool persistent, int sms, LoadOps ops) {
     uint64_t tiles = (batch << (logn - d.logr)) / (uint64_t)d.cols;
     if (tiles == 0) return cudaSuccess;
+    // the 8-column first pass stores 16-byte pairs
+    if (d.cols < kCols && ((uintptr_t)out & 15u)) return cudaErrorMisalignedAddress;
     int logp = d.logp;
     if (persistent && d.fn_persistent && d.persist_ctas_per_sm > 0 && sms > 0) {
         const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)d.persist_ctas_per_sm * (uint64_t)sms);

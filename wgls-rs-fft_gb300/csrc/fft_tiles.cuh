@@ -281,7 +281,19 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
             }
         __syncthreads();
         float2 *blk = a.dst + (uint64_t)j0 * R;
-        if (a.keep_l2) {
+        if constexpr (CL < kColsLog) {
+            // the staging swizzle (column << (4 - CL)) keeps bit 0 of q, so samples q, q + 1
+            // (q even) stay adjacent: 16-byte loads and stores, half the store
+            // instructions (the caller's dst is 16-byte aligned)
+#pragma unroll
+            for (int e = 0; e < E / 2; ++e) {
+                const int lin = 2 * (lt + COLS * T * e);
+                const int cc = lin >> LOGR, q = lin & (R - 1);
+                const float4 w = *reinterpret_cast<const float4 *>(buf + cc * R + (q ^ (cc << (kColsLog - CL))));
+                if (a.keep_l2) __stcg(reinterpret_cast<float4 *>(blk + lin), w);
+                else st_stream(reinterpret_cast<float4 *>(blk + lin), w);
+            }
+        } else if (a.keep_l2) {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 const int lin = lt + COLS * T * e;

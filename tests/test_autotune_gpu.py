@@ -206,6 +206,31 @@ def test_three_pass_first_pass_8_columns(tmp_path, monkeypatch, oracle, lib_buil
         assert oracle.rel_l2(outs[3][0], ref) <= TOL_REL_L2
 
 
+def test_three_pass_first_pass_unaligned_input(oracle, lib_built):
+    """The device entry takes any 8-byte aligned input.  For N = 2^25 (three
+    passes, the 8-column first pass, whose 16-byte stores go to the plan's
+    workspace) an input one sample past a 16-byte boundary gives the same bits
+    as the aligned host path."""
+    torch = pytest.importorskip("torch")
+    import numpy as np
+
+    import gbfft
+    from gbfft import signals
+    n = 1 << 25
+    x = signals.normal_c64(1, n, seed=1400)
+    buf = torch.empty(n + 1, dtype=torch.complex64, device="cuda")
+    buf[1:] = torch.from_numpy(x[0]).cuda()
+    dx = buf[1:]
+    assert dx.data_ptr() % 16 == 8
+    dy = torch.empty(n, dtype=torch.complex64, device="cuda")
+    with gbfft.Context(0) as ctx:
+        for d in (gbfft.FORWARD, gbfft.INVERSE):
+            aligned = ctx.c2c_host(x, d)
+            ctx.c2c_device(dx, dy, n, 1, d)
+            torch.cuda.synchronize()
+            assert np.array_equal(dy.cpu().numpy()[None], aligned)
+
+
 @pytest.mark.parametrize("logn,batch,loge", [(21, 3, 4), (22, 2, 4), (25, 1, 5)])
 def test_three_pass_persistent_first_pass(tmp_path, monkeypatch, oracle, lib_built, logn, batch, loge):
     """Three-pass plans whose lone first pass runs as a persistent tile loop

@@ -214,8 +214,9 @@ int gbfft_set_noise(gbfft_ctx *ctx, uint32_t seed, float sigma);
 /* Autotuner (no reference counterpart; the reference's find_optimal_batch
  * example only sweeps batch sizes, examples/find_optimal_batch.rs:28).  Times
  * every plan variant for (n, batch, direction, current precision) -- global
- * pass split, plain or persistent tile-loop kernels, fused pass pairs, and
- * transforms per CTA of the single-pass kernel -- on the context's own
+ * pass split, plain or persistent tile-loop kernels, fused pass pairs,
+ * transforms per CTA of the single-pass kernel, columns per CTA of a
+ * three-pass first pass, 16 or 32 samples a thread -- on the context's own
  * scratch buffers (caller data is never touched), keeps the fastest for later
  * calls with that size, direction, precision and a batch of the same power of
  * two, and writes the mean seconds per transform of the winner.  If the

@@ -295,7 +295,8 @@ def run_ragged(args, ctx, dev, rank, world):
             "tc_tf32": gbfft.PREC_TC_TF32}[args.precision]
     ctx.set_precision(prec)  # the plan takes the context's precision
     plan = ctx.ragged_plan(descs)
-    # the uniform comparison: the split form where the uniform entry has it (N >= 2^15)
+    # the uniform comparison uses the split form where the ragged kernel does (its two-pass
+    # items, N >= 2^15); the ragged kernel's single-pass groups stay FP32, so do these
     ctx_small = gbfft.Context(dev.index or 0)
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream

@@ -102,7 +102,10 @@ int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows,
 
 /* Device-resident entry point (new; no reference counterpart -- the reference
  * always round-trips through host memory).  `d_in`/`d_out` are device
- * pointers to batch*n interleaved complex<f32>; they may alias.  Work is
+ * pointers to batch*n interleaved complex<f32>; they may alias and need only
+ * the alignment of complex<f32> (8 bytes: every kernel reads and writes
+ * caller memory one sample at a time; wider accesses touch only the
+ * library's own buffers).  Work is
  * enqueued on `stream` (a cudaStream_t; NULL is the CUDA default stream, as
  * everywhere in CUDA) and the call returns without synchronising. */
 int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,

@@ -194,7 +194,7 @@ __device__ __forceinline__ void subpass_run(float2 (&v)[SubCfg<LOGN, LE>::E], in
 // Position (within the transform) of output q of butterfly slot b after
 // sub-pass (LOGR, LOGP): (j / p) R p + (j mod p) + q p.
 template <int LOGR, int LOGP, int LOGT>
-__device__ __forceinline__ int subpass_out_pos(int t, int b, int q) {
+GBFFT_HD int subpass_out_pos(int t, int b, int q) {
     const int j = t + (b << LOGT);
     return ((j >> LOGP) << (LOGR + LOGP)) + (j & ((1 << LOGP) - 1)) + (q << LOGP);
 }

@@ -127,9 +127,21 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
 // permutes every aligned group of four rows within itself, so the reads of rows
 // t + T e stay conflict-free.
 template <int CL, int PP, int PR>
-__device__ __forceinline__ int xrow(int row) {
+GBFFT_HD int xrow(int row) {
     if constexpr (CL < kColsLog && PP == 0) return row ^ ((row >> PR) & 1);
     else return row;
+}
+// Exchange-tile index of (row, column c) after a sub-pass (PR, PP).
+template <int CL, int PP, int PR>
+GBFFT_HD int xch_idx(int row, int c) {
+    return (xrow<CL, PP, PR>(row) << CL) + c;
+}
+// A first pass stages output `pos` of column c at [column][pos ^ (column << (4 - CL))]:
+// a warp's 32 / 2^CL rows of 2^CL columns then cover every bank pair twice, and
+// with CL < 4 the XOR keeps bit 0, so samples pos, pos + 1 (pos even) stay adjacent.
+template <int CL, int LOGR>
+GBFFT_HD int stage_idx(int c, int pos) {
+    return (c << LOGR) + (pos ^ (c << (kColsLog - CL)));
 }
 
 template <int LOGR, int I, int LE = 4, int CL = kColsLog, bool DONE = (I >= SubCfg<LOGR, LE>::NSUB)>
@@ -144,10 +156,10 @@ struct PassChain {
         for (int b = 0; b < (C::E >> PR); ++b)
 #pragma unroll
             for (int q = 0; q < (1 << PR); ++q)
-                buf[(xrow<CL, PP, PR>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q)) << CL) + c] = v[b + q * (C::E >> PR)];
+                buf[xch_idx<CL, PP, PR>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), c)] = v[b + q * (C::E >> PR)];
         __syncthreads();
 #pragma unroll
-        for (int e = 0; e < C::E; ++e) v[e] = buf[(xrow<CL, PP, PR>(t + C::T * e) << CL) + c];
+        for (int e = 0; e < C::E; ++e) v[e] = buf[xch_idx<CL, PP, PR>(t + C::T * e, c)];
         subpass_run<LOGR, I, LE>(v, t, tw, eng);
         PassChain<LOGR, I + 1, LE, CL>::run(v, t, c, buf, tw, eng);
     }
@@ -267,29 +279,27 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
     constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);
     constexpr int NB = E >> LR;
     if (FIRST) {
-        // Outputs of column j are contiguous at j R + q: stage them as
-        // [column][q ^ (column << (4 - CL))] (a warp's 32 / 2^CL rows of 2^CL
-        // columns then cover every bank pair twice) and store each group's
-        // 2^CL R-sample block linearly.
+        // Outputs of column j are contiguous at j R + q: stage them (stage_idx)
+        // and store each group's 2^CL R-sample block linearly.
         __syncthreads();
 #pragma unroll
         for (int bb = 0; bb < NB; ++bb)
 #pragma unroll
             for (int q = 0; q < (1 << LR); ++q) {
                 const int pos = subpass_out_pos<LR, LP, C::LOGT>(t, bb, q);
-                buf[c * R + (pos ^ (c << (kColsLog - CL)))] = v[bb + q * NB];
+                buf[stage_idx<CL, LOGR>(c, pos)] = v[bb + q * NB];
             }
         __syncthreads();
         float2 *blk = a.dst + (uint64_t)j0 * R;
         if constexpr (CL < kColsLog) {
-            // the staging swizzle (column << (4 - CL)) keeps bit 0 of q, so samples q, q + 1
-            // (q even) stay adjacent: 16-byte loads and stores, half the store
-            // instructions (the caller's dst is 16-byte aligned)
+            // samples q, q + 1 (q even) are adjacent in the staging buffer: 16-byte
+            // loads and stores, half the store instructions (the caller's dst is
+            // 16-byte aligned)
 #pragma unroll
             for (int e = 0; e < E / 2; ++e) {
                 const int lin = 2 * (lt + COLS * T * e);
                 const int cc = lin >> LOGR, q = lin & (R - 1);
-                const float4 w = *reinterpret_cast<const float4 *>(buf + cc * R + (q ^ (cc << (kColsLog - CL))));
+                const float4 w = *reinterpret_cast<const float4 *>(buf + stage_idx<CL, LOGR>(cc, q));
                 if (a.keep_l2) __stcg(reinterpret_cast<float4 *>(blk + lin), w);
                 else st_stream(reinterpret_cast<float4 *>(blk + lin), w);
             }
@@ -298,14 +308,14 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
             for (int e = 0; e < E; ++e) {
                 const int lin = lt + COLS * T * e;
                 const int cc = lin >> LOGR, q = lin & (R - 1);
-                __stcg(blk + lin, buf[cc * R + (q ^ (cc << (kColsLog - CL)))]);
+                __stcg(blk + lin, buf[stage_idx<CL, LOGR>(cc, q)]);
             }
         } else {
 #pragma unroll
             for (int e = 0; e < E; ++e) {
                 const int lin = lt + COLS * T * e;
                 const int cc = lin >> LOGR, q = lin & (R - 1);
-                st_stream(blk + lin, buf[cc * R + (q ^ (cc << (kColsLog - CL)))]);
+                st_stream(blk + lin, buf[stage_idx<CL, LOGR>(cc, q)]);
             }
         }
     } else {

@@ -1,14 +1,18 @@
-// Host-side check of the global-pass tile's shared-memory index maps
-// (fft_tiles.cuh: subpass_out_pos, xch_idx, stage_idx), compiled for the host
-// by nvcc and run by tests/test_tile_maps.py.  For every tile the kernels use
-// (radix 2^LOGR, 2^LE samples a thread, 2^CL columns):
+// Host-side check of the shared-memory index maps of the single-pass tile
+// (fft_tiles.cuh: subpass_out_pos, swz) and of the global-pass tile
+// (subpass_out_pos, xch_idx, stage_idx), compiled for the host by nvcc and run
+// by tests/test_tile_maps.py.  Single-pass tiles (N = 2^LOGN, 2^LE samples a
+// thread): every exchange is a bijection onto the transform's N slots, read back
+// where it was written; worst wavefronts of a warp (which spans 32 / T
+// transforms when T < 32).  Prints: rows LOGN LE ok wavefronts.
+// Global-pass tiles (radix 2^LOGR, 2^LE samples a thread, 2^CL columns):
 //   * each exchange after a sub-pass writes every slot of the [row][column]
 //     tile once, in bounds, and the next sub-pass reads back (column, row);
 //   * a first pass's output staging is a bijection, read back in linear order
 //     (as 16-byte pairs when CL < 4);
 //   * the worst shared-memory wavefronts of one warp access (8-byte lanes need
 //     at least 2, 16-byte lanes 4).
-// Prints one line a tile: LOGR LE CL ok exchange_wavefronts staging_wavefronts pair_wavefronts.
+// Prints: pass LOGR LE CL ok exchange_wavefronts staging_wavefronts pair_wavefronts.
 #include <algorithm>
 #include <cstdio>
 #include <map>
@@ -122,10 +126,76 @@ void check_tile() {
             }
             wp = std::max(wp, wavefronts(a));
         }
-    printf("%d %d %d %d %d %d %d\n", LOGR, LE, CL, ok ? 1 : 0, wx, ws, wp);
+    printf("pass %d %d %d %d %d %d %d\n", LOGR, LE, CL, ok ? 1 : 0, wx, ws, wp);
+}
+
+template <int LOGN, int LE, int I>
+void check_rows_exchanges(bool &ok, int &worst) {
+    using C = SubCfg<LOGN, LE>;
+    if constexpr (I < C::NSUB) {
+        constexpr int PR = C::logr(I - 1), PP = C::logp(I - 1);
+        constexpr int N = C::N, T = C::T, E = C::E;
+        constexpr int G = T >= 32 ? 1 : 32 / T;  // transforms one warp spans
+        std::vector<int> owner(N, -1);
+        for (int t = 0; t < T; ++t)
+            for (int b = 0; b < (E >> PR); ++b)
+                for (int q = 0; q < (1 << PR); ++q) {
+                    const int pos = subpass_out_pos<PR, PP, C::LOGT>(t, b, q);
+                    const int i = swz<C::LOGE>(pos, PP);
+                    if (pos < 0 || pos >= N || i < 0 || i >= N || owner[i] != -1) ok = false;
+                    else owner[i] = pos;
+                }
+        for (int t = 0; t < T; ++t)
+            for (int e = 0; e < E; ++e) {
+                const int i = swz<C::LOGE>(t + T * e, PP);
+                if (i < 0 || i >= N || owner[i] != t + T * e) ok = false;
+            }
+        for (int w = 0; w < (G * T) / 32 || w == 0; ++w) {
+            for (int b = 0; b < (E >> PR); ++b)
+                for (int q = 0; q < (1 << PR); ++q) {
+                    std::vector<int> a;
+                    for (int l = 0; l < 32; ++l) {
+                        const int tid = 32 * w + l, g = tid / T, t = tid % T;
+                        a.push_back(g * N + swz<C::LOGE>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP));
+                    }
+                    worst = std::max(worst, wavefronts(a));
+                }
+            for (int e = 0; e < E; ++e) {
+                std::vector<int> a;
+                for (int l = 0; l < 32; ++l) {
+                    const int tid = 32 * w + l, g = tid / T, t = tid % T;
+                    a.push_back(g * N + swz<C::LOGE>(t + T * e, PP));
+                }
+                worst = std::max(worst, wavefronts(a));
+            }
+            if (T > 32 && w + 1 >= T / 32) break;
+        }
+        check_rows_exchanges<LOGN, LE, I + 1>(ok, worst);
+    }
+}
+
+template <int LOGN, int LE>
+void check_rows() {
+    bool ok = true;
+    int w = 0;
+    check_rows_exchanges<LOGN, LE, 1>(ok, w);
+    printf("rows %d %d %d %d\n", LOGN, LE, ok ? 1 : 0, w);
 }
 
 int main() {
+    check_rows<4, 4>();
+    check_rows<5, 4>();
+    check_rows<6, 4>();
+    check_rows<7, 4>();
+    check_rows<8, 4>();
+    check_rows<9, 4>();
+    check_rows<10, 4>();
+    check_rows<11, 4>();
+    check_rows<12, 4>();
+    check_rows<13, 4>();
+    check_rows<14, 4>();
+    check_rows<13, 5>();
+    check_rows<14, 5>();
     // 16 columns: every pass radix with 16 samples a thread, 2^7..2^10 with 32
     check_tile<5, 4, 4>();
     check_tile<6, 4, 4>();

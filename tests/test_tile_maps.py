@@ -1,12 +1,17 @@
-"""CPU: the shared-memory index maps of the global-pass tile (fft_tiles.cuh) for
-every tile the kernels use -- radix 2^5..2^10 with 16 samples a thread, 2^7..2^10
-with 32, and the 8-column first pass of radix 2^9 / 2^10 -- compiled for the
-host by nvcc from the kernels' own index functions (no GPU needed).
+"""CPU: the shared-memory index maps of the single-pass tile and the global-pass
+tile (fft_tiles.cuh) for every tile the kernels use -- single pass N = 2^4..2^14
+with 16 samples a thread and 2^13 / 2^14 with 32; global passes of radix
+2^5..2^10 with 16 samples a thread, 2^7..2^10 with 32, and the 8-column first
+pass of radix 2^9 / 2^10 -- compiled for the host by nvcc from the kernels' own
+index functions (no GPU needed).
 
 Checked: every exchange and the first-pass output staging are bijections onto
 the tile, read back where they were written (the staging as adjacent 16-byte
 pairs for 8 columns), and each warp access takes the fewest shared-memory
-wavefronts its width allows (2 for 8-byte lanes, 4 for 16-byte lanes)."""
+wavefronts its width allows (2 for 8-byte lanes, 4 for 16-byte lanes).  The
+one known exception is pinned: single-pass N = 2^5 / 2^6 / 2^7, where a warp
+spans 16 / 8 / 4 transforms whose buffers start on the same banks (16, 8 and
+4 wavefronts)."""
 import os
 import shutil
 import subprocess
@@ -28,9 +33,14 @@ def test_pass_tile_index_maps(tmp_path):
                         "-I", CSRC, SRC, "-o", exe], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines()
-    rows = [tuple(int(v) for v in line.split()) for line in out]
-    assert len(rows) == 14
-    for logr, le, cl, ok, wx, ws, wp in rows:
+    single = [tuple(int(v) for v in line.split()[1:]) for line in out if line.startswith("rows ")]
+    passes = [tuple(int(v) for v in line.split()[1:]) for line in out if line.startswith("pass ")]
+    assert len(single) == 13 and len(passes) == 14
+    small = {4: 0, 5: 16, 6: 8, 7: 4}  # no exchange at 2^4; warps spanning several transforms below 2^8
+    for logn, le, ok, w in single:
+        assert ok == 1, (logn, le)
+        assert w == small.get(logn, 2), ("single-pass exchange wavefronts", logn, le, w)
+    for logr, le, cl, ok, wx, ws, wp in passes:
         assert ok == 1, (logr, le, cl)
         assert wx == 2, ("exchange wavefronts", logr, le, cl, wx)
         assert ws == 2, ("staging wavefronts", logr, le, cl, ws)

@@ -19,7 +19,7 @@ constexpr int kCols = 1 << kColsLog;
 // p < 2^LE the low LE bits are XORed with (a >> LE) << logp (a bijection), which
 // spreads the stride-p writes over the banks.
 template <int LE = 4>
-__device__ __forceinline__ int swz(int a, int logp) {
+GBFFT_HD int swz(int a, int logp) {
     return logp < LE ? (a ^ (((a >> LE) << logp) & ((1 << LE) - 1))) : a;
 }
 

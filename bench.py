@@ -246,31 +246,60 @@ def run_reference_arm(args, workload):
     rank, world, _ = rank_info()
     if rank != 0:
         return 0
-    logn, batch, dist, seed = WORKLOADS[workload]
-    n = 1 << logn
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
+    import gbfft
     from gbfft import signals
     oracle.build()
     threads = os.cpu_count() or 1
-    rows = max(threads, min(batch, 256 if n <= 4096 else max(1, (1 << 20) // n)))
-    x = signals.normal_c64(rows, n, seed=seed) if dist == "normal" else signals.uniform_c64(rows, n, seed=seed)
+    what = "reference Stockham R4/R2 f32 path restated in C"
+    if workload == "ragged_c5":
+        # a bounded sample of the ragged set: its transforms in descriptor order up
+        # to 2^22 samples a step, each (size, direction) group run as one batch
+        descs, total = signals.ragged_set(args.ragged_count, seed=5)
+        groups, samples, count = {}, 0, 0
+        for L, d in zip(descs["log2n"].tolist(), descs["direction"].tolist()):
+            if samples >= (1 << 22):
+                break
+            groups[(L, d)] = groups.get((L, d), 0) + 1
+            samples += 1 << L
+            count += 1
+        jobs = [(signals.uniform_c64(b, 1 << L, seed=5 + L), d == gbfft.INVERSE) for (L, d), b in sorted(groups.items())]
+
+        def step():
+            for x, inv in jobs:
+                oracle.ref_fft(x, inv, threads)
+        sample = f"the first {count} of {len(descs)} transforms ({samples} samples) per step, {what}, {threads} threads"
+        data = "synthetic (seeded PCG hash, re/im iid U[-1,1))"
+        config = {"workload": workload, "transforms": len(descs), "log2n": "uniform 8..18", "directions": "50/50",
+                  "total_samples": total, "l2": "n/a (host)"}
+    else:
+        logn, batch, dist, seed = WORKLOADS[workload]
+        n = 1 << logn
+        rows = max(threads, min(batch, 256 if n <= 4096 else max(1, (1 << 20) // n)))
+        gen = {"normal": signals.normal_c64, "uniform": signals.uniform_c64, "tones": signals.tones_c64}[dist]
+        x = gen(rows, n, seed=seed)
+
+        def step():
+            oracle.ref_fft(oracle.ref_fft(x, False, threads), True, threads)
+        samples = 2 * rows * n
+        sample = f"{rows} of {batch} rows of N={n} per step (forward + inverse), {what}, {threads} threads"
+        data = "synthetic (seeded PCG hash, " + {"normal": "re/im iid N(0,1))", "uniform": "re/im iid U[-1,1))",
+                                                 "tones": "64 tones 10^U[-3,3] + N(0,1e-2) noise)"}[dist]
+        config = {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse", "l2": "n/a (host)"}
     for _ in range(args.warmup):
-        oracle.ref_fft(oracle.ref_fft(x, False, threads), True, threads)
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.ref_fft(oracle.ref_fft(x, False, threads), True, threads)
+        step()
     el = time.perf_counter() - t0
-    value = 2.0 * rows * n * args.steps / el / 1e9
-    sample = (f"{rows} of {batch} rows of N={n} per step (forward + inverse), "
-              f"reference Stockham R4/R2 f32 path restated in C, {threads} threads")
+    value = samples * args.steps / el / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded PCG, N(0,1))",
-        "config": {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse",
-                   "l2": "n/a (host)"},
+        "data": data,
+        "config": config,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,

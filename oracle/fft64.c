@@ -13,6 +13,7 @@
  * autosort in double (O(N log N)); fft64_dft is the O(N^2) direct sum that
  * pins it for N <= 4096.
  */
+#define _GNU_SOURCE /* pthread_barrier_t under -std=c11 */
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
@@ -112,6 +113,87 @@ static void *f64_worker(void *arg)
     return NULL;
 }
 
+/* One long transform split over threads stage by stage (batches smaller than
+ * the thread count, e.g. a single 2^26-point row): each thread takes a
+ * contiguous range of butterflies of every radix-2 stage, with a barrier
+ * between stages.  Same arithmetic as stockham64, so the same result. */
+typedef struct {
+    const float *in_f;
+    const double *in_d;
+    double *out, *x, *y, *tw;
+    uint64_t n, row;
+    int inverse, t, threads;
+    pthread_barrier_t *bar;
+} f64_stage_job;
+
+static void *f64_stage_worker(void *arg)
+{
+    f64_stage_job *j = (f64_stage_job *)arg;
+    uint64_t n = j->n, half = n >> 1;
+    uint64_t lo = half * (uint64_t)j->t / (uint64_t)j->threads;
+    uint64_t hi = half * (uint64_t)(j->t + 1) / (uint64_t)j->threads;
+    for (uint64_t i = 2 * lo; i < 2 * hi; ++i) { /* load this thread's share of the row */
+        uint64_t a = i, b = i + n;
+        j->x[a] = j->in_f ? (double)j->in_f[j->row * 2 * n + a] : j->in_d[j->row * 2 * n + a];
+        j->x[b] = j->in_f ? (double)j->in_f[j->row * 2 * n + b] : j->in_d[j->row * 2 * n + b];
+    }
+    pthread_barrier_wait(j->bar);
+    double *src = j->x, *dst = j->y;
+    for (uint64_t p = 1; p < n; p <<= 1) {
+        for (uint64_t tid = lo; tid < hi; ++tid) {
+            uint64_t k = tid & (p - 1), jj = tid / p;
+            uint64_t i1 = jj * p + k, i2 = i1 + half;
+            double ar = src[2 * i1], ai = src[2 * i1 + 1];
+            double br = src[2 * i2], bi = src[2 * i2 + 1];
+            uint64_t t = k * (half / p);
+            double wr = j->tw[2 * t], wi = j->tw[2 * t + 1];
+            if (j->inverse)
+                wi = -wi;
+            double tr = wr * br - wi * bi, ti = wr * bi + wi * br;
+            uint64_t d = 2 * (jj * 2 * p + k);
+            dst[d] = ar + tr;
+            dst[d + 1] = ai + ti;
+            dst[d + 2 * p] = ar - tr;
+            dst[d + 2 * p + 1] = ai - ti;
+        }
+        pthread_barrier_wait(j->bar);
+        double *tmp = src; src = dst; dst = tmp;
+    }
+    double sc = j->inverse ? 1.0 / (double)n : 1.0;
+    for (uint64_t i = 2 * lo; i < 2 * hi; ++i) {
+        j->out[j->row * 2 * n + i] = src[i] * sc;
+        j->out[j->row * 2 * n + i + n] = src[i + n] * sc;
+    }
+    return NULL;
+}
+
+static int fft64_rows_stage_parallel(const float *in_f, const double *in_d, double *out, double *tw,
+                                     uint64_t n, uint64_t batch, int inverse, int threads)
+{
+    double *x = (double *)malloc(n * 2 * sizeof(double));
+    double *y = (double *)malloc(n * 2 * sizeof(double));
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);
+    f64_stage_job *jobs = (f64_stage_job *)malloc(sizeof(f64_stage_job) * threads);
+    int rc = 0;
+    if (!x || !y || !th || !jobs) {
+        rc = -2;
+    } else {
+        pthread_barrier_t bar;
+        for (uint64_t r = 0; r < batch; ++r) {
+            pthread_barrier_init(&bar, NULL, (unsigned)threads);
+            for (int t = 0; t < threads; ++t) {
+                jobs[t] = (f64_stage_job){in_f, in_d, out, x, y, tw, n, r, inverse, t, threads, &bar};
+                pthread_create(&th[t], NULL, f64_stage_worker, &jobs[t]);
+            }
+            for (int t = 0; t < threads; ++t)
+                pthread_join(th[t], NULL);
+            pthread_barrier_destroy(&bar);
+        }
+    }
+    free(x); free(y); free(th); free(jobs);
+    return rc;
+}
+
 static int fft64_batch_impl(const float *in_f, const double *in_d, double *out,
                             uint64_t n, uint64_t batch, int inverse, int threads)
 {
@@ -124,6 +206,11 @@ static int fft64_batch_impl(const float *in_f, const double *in_d, double *out,
         fft64_twiddle(j, n, &tw[2 * j], &tw[2 * j + 1]);
     if (threads < 1)
         threads = 1;
+    if ((uint64_t)threads > 2 * batch && n >= (1u << 16) && (uint64_t)threads <= n / 2) {
+        int rc = fft64_rows_stage_parallel(in_f, in_d, out, tw, n, batch, inverse, threads);
+        free(tw);
+        return rc;
+    }
     if ((uint64_t)threads > batch)
         threads = (int)(batch ? batch : 1);
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * threads);

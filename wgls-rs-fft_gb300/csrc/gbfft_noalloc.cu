@@ -1,13 +1,15 @@
 // gbfft_c2c_device_noalloc: the two-pass transform (N = 2^15 .. 2^20) for
 // callers that cannot allocate GPU memory.
 //
-// Who needs it: code that runs where cudaMalloc is off limits -- inside a host
-// callback or another library's allocator hook, in a process whose device
-// memory is fully reserved by a pool it does not own, or in real-time paths
-// where an allocation (and the implicit synchronisation cudaFree brings) would
-// stall.  The regular entry points allocate on first use of a size (twiddle
-// tables, a workspace); this one never calls cudaMalloc, cudaFree or any
-// allocating library routine.
+// Who needs it: code that must not call cudaMalloc -- another library's
+// allocator hook (an allocation from inside it would re-enter the allocator),
+// a process whose device memory is fully reserved by a pool it does not own,
+// or a real-time path where an allocation (and the implicit synchronisation
+// cudaFree brings) would stall.  The regular entry points allocate on first
+// use of a size (twiddle tables, a workspace); this one never calls
+// cudaMalloc, cudaFree or any allocating library routine.  (It does launch
+// kernels, so it is no more usable than any other CUDA call from places where
+// CUDA forbids API calls, such as a stream's host callback.)
 //
 // Where its memory comes from: two file-scope device arrays of this library,
 // a 32 MiB scratch buffer for the intermediate result between the two global
@@ -15,17 +17,25 @@
 // The driver reserves them when it loads this library's code on a GPU; every
 // GPU that loads the library holds them until the process exits.
 //
+// Speed: it runs one launch per global pass with 16 samples a thread, the
+// plain two-pass schedule.  The regular device entry runs both passes in one
+// fused launch at these sizes (32 samples a thread from 2^17), which is
+// 10-15 % faster; this entry trades that for needing no workspace.
+//
 // Set-up: the first call on each device (with that device current) looks up
 // the arrays' device addresses with cudaGetSymbolAddress, fills the twiddle
 // tables for all supported sizes and synchronises the caller's stream.  Make
 // that first call before any stream capture.  Later calls only enqueue the two
-// pass kernels on the caller's stream.
+// pass kernels on the caller's stream.  The set-up is done once per device for
+// the life of the process: after a cudaDeviceReset the arrays are re-created
+// empty and this entry must not be called again on that device.
 //
 // Sharing: every call on a device uses the same scratch array, which keeps
 // whatever the previous call left in it.  Nothing in it needs to start at
 // zero (the first pass overwrites every sample the second pass reads).  Calls
 // that overlap on the GPU (different streams, or concurrent host threads) race
 // on the scratch array: serialise them.
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -50,15 +60,19 @@ struct NaPlan {
     int split = 0;
 };
 
+// Per-device state.  `ready` is published with release order after the set-up
+// has filled the rest, so a call that reads it true with acquire order sees
+// the addresses and plans without taking the lock; `mu` serialises the set-up
+// of one device only.
 struct NaDevice {
-    bool ready = false;
+    std::atomic<bool> ready{false};
+    std::mutex mu;
     float2 *scratch = nullptr;
     float2 *tw = nullptr;
     NaPlan plan[kNaMaxLogN + 1];
 };
 
 NaDevice g_na_dev[kNaMaxDevices];
-std::mutex g_na_mu;
 
 int na_setup(int dev, cudaStream_t stream, NaDevice &d) {
     void *p = nullptr;
@@ -93,7 +107,7 @@ int na_setup(int dev, cudaStream_t stream, NaDevice &d) {
         if (twiddle_fill(d.tw, segs.data(), (int)segs.size(), stream) != cudaSuccess) return GBFFT_ERR_CUDA;
     }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return GBFFT_ERR_CUDA;
-    d.ready = true;
+    d.ready.store(true, std::memory_order_release);
     (void)dev;
     return GBFFT_OK;
 }
@@ -120,9 +134,9 @@ extern "C" int gbfft_c2c_device_noalloc(const void *d_in, void *d_out, uint64_t 
     }
     cudaStream_t s = (cudaStream_t)stream;
     NaDevice &d = g_na_dev[dev];
-    {
-        std::lock_guard<std::mutex> lock(g_na_mu);
-        if (!d.ready) {
+    if (!d.ready.load(std::memory_order_acquire)) {
+        std::lock_guard<std::mutex> lock(d.mu);
+        if (!d.ready.load(std::memory_order_relaxed)) {
             int st = na_setup(dev, s, d);
             if (st != GBFFT_OK) return st;
         }

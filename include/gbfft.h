@@ -92,10 +92,14 @@ int gbfft_c2c_host(gbfft_ctx *ctx, const float *in, float *out, uint64_t n,
  * (src/lib.rs:433, 517-533): `batch` separate rows, row i at in_rows[i] with
  * row_lengths[i] complex values, result row i written to out_rows[i].
  * All lengths must be equal (GBFFT_ERR_LENGTH_MISMATCH) and a power of two
- * (GBFFT_ERR_INVALID_SIZE), checked in the reference's order.  Rows are
- * copied to and from pinned staging chunk by chunk while earlier chunks are
- * on the device, so out_rows[i] may be in_rows[i] (in place) but must not
- * overlap any other input row. */
+ * (GBFFT_ERR_INVALID_SIZE), checked in the reference's order.  Where the
+ * device reaches pageable host memory through the host's page tables
+ * (cudaDevAttrPageableMemoryAccess: NVLink-C2C on Grace), the GPU gathers the
+ * rows into device memory and scatters the results into out_rows itself,
+ * chunk by chunk; elsewhere they are copied through pinned staging on host
+ * threads.  Either way out_rows[i] may be in_rows[i] (in place) but must not
+ * overlap any other input row.  The same applies to gbfft_c2c_host with a
+ * pageable (not cudaHostAlloc'd) batch. */
 int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows,
                         const uint64_t *row_lengths, float *const *out_rows,
                         uint64_t batch, int direction);
@@ -112,11 +116,13 @@ int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,
                      uint64_t batch, int direction, void *stream);
 
 /* Allocation-free variant of gbfft_c2c_device (no counterpart in the
- * reference).  For callers that may not allocate GPU memory -- code running in
- * a host callback or an allocator hook, under a memory pool that owns all of
- * the device's memory, or on a latency path where cudaMalloc/cudaFree and the
- * synchronisation they imply are not acceptable.  It never calls cudaMalloc,
- * cudaFree or any allocating routine, and it needs no context.
+ * reference).  For callers that may not allocate GPU memory -- code inside
+ * another library's allocator hook (allocating there would re-enter the
+ * allocator), under a memory pool that owns all of the device's memory, or on
+ * a latency path where cudaMalloc/cudaFree and the synchronisation they imply
+ * are not acceptable.  It never calls cudaMalloc, cudaFree or any allocating
+ * routine, and it needs no context.  It launches kernels, so like any CUDA
+ * call it must not be made from a stream's host callback.
  *
  * Limits: n a power of two with 2^15 <= n <= 2^20 and n * batch <= 2^22
  * (the library's built-in 32 MiB scratch array); anything larger or smaller
@@ -124,8 +130,12 @@ int gbfft_c2c_device(gbfft_ctx *ctx, const void *d_in, void *d_out, uint64_t n,
  * Device pointers and stream as for gbfft_c2c_device; runs on the current
  * device.  The first call on each device sets up (looks up the scratch and
  * twiddle arrays and fills the tables) and synchronises `stream`: make that
- * first call before any stream capture.  All calls on a device share the one
- * scratch array, so calls that overlap on the GPU race: serialise them. */
+ * first call before any stream capture; the set-up is not redone after a
+ * cudaDeviceReset, so do not call this entry on a device after resetting it.
+ * All calls on a device share the one scratch array, so calls that overlap on
+ * the GPU race: serialise them.  It runs the plain two-pass schedule (one
+ * launch per pass), 10-15 % slower at these sizes than gbfft_c2c_device's
+ * fused pass pair. */
 int gbfft_c2c_device_noalloc(const void *d_in, void *d_out, uint64_t n,
                              uint64_t batch, int direction, void *stream);
 
@@ -233,6 +243,9 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
  *   GBFFT_AUTOTUNE, GBFFT_AUTOTUNE_CACHE   see gbfft_autotune
  *   GBFFT_PRECISION=tc_fp16|tc_bf16x3|tc_tf32  default precision of new contexts
  *   GBFFT_HOST_CHUNK_BYTES=<bytes>         chunk of the host-batch pipeline (32 MB)
+ *   GBFFT_HOST_PATH=staged                 pageable host batches go through pinned
+ *                                          staging even where the GPU could reach
+ *                                          them directly
  *   GBFFT_DEVICE_ALLOC_CAP=<bytes>         device requests above it fail with
  *                                          GBFFT_ERR_OUT_OF_MEMORY (tests the
  *                                          out-of-memory paths without a real one) */

@@ -426,3 +426,44 @@ def test_out_of_memory_paths(lib_built, monkeypatch, oracle, torch_cuda):
         monkeypatch.delenv("GBFFT_DEVICE_ALLOC_CAP")
         y = ctx.c2c_host(x, gbfft.FORWARD)
         assert oracle.rel_l2(y, oracle.fft64(x)) <= TOL_REL_L2
+
+
+# ---- host batches moved by the GPU through the host's page tables ----------------------
+
+@pytest.mark.parametrize("logn,batch", [(0, 5), (1, 3), (10, 700), (12, 300), (16, 40), (20, 3), (22, 2)])
+def test_host_direct_path_matches_staged(lib_built, oracle, monkeypatch, logn, batch):
+    """Pageable batches and separate rows are gathered and scattered by the GPU
+    itself (cudaDevAttrPageableMemoryAccess) instead of host memcpy through
+    pinned staging.  Both paths run the same transform, so their results are
+    bit-identical: contiguous and row batches, several chunks (2^10 x 700 is
+    5.6 MB, 2^16 x 40 is 21 MB: 32 MB chunks hold fewer rows at 2^16), rows
+    only 8-byte aligned, N = 1 and 2, in place, and a three-pass size."""
+    import gbfft
+    from gbfft import signals
+    n = 1 << logn
+    monkeypatch.setenv("GBFFT_HOST_CHUNK_BYTES", str(4 << 20))  # several chunks at these sizes
+    x = signals.uniform_c64(batch, n, seed=730 + logn)
+    monkeypatch.setenv("GBFFT_HOST_PATH", "staged")
+    with gbfft.Context(0) as staged:
+        want_f = staged.c2c_host(x, gbfft.FORWARD)
+        want_i = staged.c2c_host(x, gbfft.INVERSE)
+    monkeypatch.delenv("GBFFT_HOST_PATH")
+    with gbfft.Context(0) as ctx:
+        assert np.array_equal(ctx.c2c_host(x, gbfft.FORWARD), want_f)
+        assert np.array_equal(ctx.c2c_host(x, gbfft.INVERSE), want_i)
+        # separate rows, each allocated one sample into a larger block: 8-byte aligned only
+        blocks = [np.empty(n + 1, np.complex64) for _ in range(batch)]
+        rows = [b[1:] for b in blocks]
+        for r, v in zip(rows, x):
+            r[:] = v
+        assert all(r.ctypes.data % 16 == 8 for r in rows)
+        got = ctx.c2c_host_rows(rows, gbfft.FORWARD)
+        assert np.array_equal(np.stack(got), want_f)
+        # in place through the C ABI: the same pointer array for input and output
+        import ctypes
+        L = gbfft.load()
+        ptrs = (ctypes.c_void_p * batch)(*[r.ctypes.data for r in rows])
+        lens = (ctypes.c_uint64 * batch)(*([n] * batch))
+        assert L.gbfft_c2c_host_rows(ctx.handle, ptrs, lens, ptrs, batch, gbfft.INVERSE) == 0
+        assert np.array_equal(np.stack(rows), want_i)
+    assert oracle.rel_l2(want_f, oracle.fft64(x)) <= TOL_REL_L2

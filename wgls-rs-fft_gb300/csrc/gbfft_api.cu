@@ -121,6 +121,15 @@ struct gbfft_ctx {
     uint64_t launches = 0;
     int precision = GBFFT_PREC_FP32;
     size_t host_chunk = (size_t)32 << 20;  // bytes of a host batch per pipelined copy (GBFFT_HOST_CHUNK_BYTES)
+    // Pageable host batches and separate rows are moved by the GPU itself through
+    // the host's page tables when the device can (cudaDevAttrPageableMemoryAccess;
+    // GBFFT_HOST_PATH=staged turns it off): no host memcpy, no pinned staging.
+    bool host_direct = false;
+    int sms = 0;
+    DeviceBuffer dtable;          // device copy of the caller's row pointers (in, then out)
+    uint64_t *htable = nullptr;   // its pinned source
+    size_t htable_bytes = 0;
+    cudaEvent_t ev_table = nullptr;
 };
 
 namespace {
@@ -499,6 +508,82 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
     return check_device_flag(ctx);
 }
 
+// Host batch in pageable memory (contiguous at in_base/out_base, or separate
+// rows in_rows[r] / out_rows[r]) moved by the GPU through the host's page
+// tables: per chunk of whole transforms, one kernel gathers the chunk's rows
+// into HBM, the transform runs, one kernel scatters the result into the
+// caller's rows.  Chunks alternate over three streams so one chunk's gather,
+// another's transform and a third's scatter overlap.  Nothing runs on the host
+// but the launches; the call returns after the last chunk's scatter.
+static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, const char *in_base,
+                                char *out_base, const float *const *in_rows, float *const *out_rows) {
+    const size_t row_bytes = (size_t)n * sizeof(float2);
+    const size_t bytes = row_bytes * batch;
+    const int logn = log2u(n);
+    int st = ctx->dbuf.ensure(bytes, ctx->err);
+    if (st == GBFFT_OK) st = ctx->dbuf_out.ensure(bytes, ctx->err);
+    if (st != GBFFT_OK) return st;
+    char *d = (char *)ctx->dbuf.ptr;
+    char *dy = (char *)ctx->dbuf_out.ptr;
+    const uint64_t *tin = nullptr, *tout = nullptr;
+    uintptr_t align_bits = 0;
+    if (in_rows) {
+        const size_t tbytes = 2 * batch * sizeof(uint64_t);
+        if (ctx->htable_bytes < tbytes) {
+            if (ctx->htable) cudaFreeHost(ctx->htable);
+            ctx->htable = nullptr;
+            ctx->htable_bytes = 0;
+            cudaError_t e = cudaHostAlloc((void **)&ctx->htable, tbytes, cudaHostAllocDefault);
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return fail(ctx, GBFFT_ERR_OUT_OF_MEMORY, "pinned row table of %zu bytes: %s", tbytes,
+                            cudaGetErrorString(e));
+            }
+            ctx->htable_bytes = tbytes;
+        }
+        st = ctx->dtable.ensure(tbytes, ctx->err);
+        if (st != GBFFT_OK) return st;
+        for (uint64_t r = 0; r < batch; ++r) {
+            ctx->htable[r] = (uint64_t)(uintptr_t)in_rows[r];
+            ctx->htable[batch + r] = (uint64_t)(uintptr_t)out_rows[r];
+            align_bits |= (uintptr_t)in_rows[r] | (uintptr_t)out_rows[r];
+        }
+        GB_CUDA(ctx, cudaMemcpyAsync(ctx->dtable.ptr, ctx->htable, tbytes, cudaMemcpyHostToDevice, ctx->xfer[0]));
+        GB_CUDA(ctx, cudaEventRecord(ctx->ev_table, ctx->xfer[0]));
+        GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[1], ctx->ev_table, 0));
+        GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[2], ctx->ev_table, 0));
+        tin = (const uint64_t *)ctx->dtable.ptr;
+        tout = tin + batch;
+    } else {
+        align_bits = (uintptr_t)in_base | (uintptr_t)out_base;
+    }
+    const bool vec16 = logn >= 1 && (align_bits & 15) == 0;
+    uint64_t rows_per_chunk = row_bytes >= ctx->host_chunk ? 1 : ctx->host_chunk / row_bytes;
+    if (logn > kRowsMaxLogN && rows_per_chunk < batch) {
+        // plans of three or more passes share the context's workspace: one chunk
+        const PlanVariant v = choose_variant(ctx, logn, rows_per_chunk, direction, st);
+        Plan *plan = nullptr;
+        if (st == GBFFT_OK) st = get_plan(ctx, logn, v, &plan);
+        if (st != GBFFT_OK) return st;
+        if (plan->passes.size() >= 3) rows_per_chunk = batch;
+    }
+    size_t c = 0;
+    for (uint64_t r0 = 0; r0 < batch; r0 += rows_per_chunk, ++c) {
+        const uint64_t rows = std::min(batch - r0, rows_per_chunk);
+        const size_t off = (size_t)r0 * row_bytes;
+        cudaStream_t s = ctx->xfer[c % 3];
+        GB_CUDA(ctx, host_rows_copy(tin ? tin + r0 : nullptr, (void *)(in_base ? in_base + off : nullptr), rows, logn,
+                                    d + off, true, vec16, ctx->sms, s));
+        st = run_device(ctx, (const float2 *)(d + off), (float2 *)(dy + off), n, rows, direction, s, r0);
+        if (st != GBFFT_OK) return st;
+        GB_CUDA(ctx, host_rows_copy(tout ? tout + r0 : nullptr, (void *)(out_base ? out_base + off : nullptr), rows,
+                                    logn, dy + off, false, vec16, ctx->sms, s));
+        ctx->launches += 2;
+    }
+    for (auto &s : ctx->xfer) GB_CUDA(ctx, cudaStreamSynchronize(s));
+    return check_device_flag(ctx);
+}
+
 }  // namespace
 
 extern "C" {
@@ -563,6 +648,15 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
         ctx->tune_cache = c;
         load_tune_cache(ctx.get());
     }
+    if (cudaEventCreateWithFlags(&ctx->ev_table, cudaEventDisableTiming) != cudaSuccess) return GBFFT_ERR_CUDA;
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    int pageable = 0;
+    if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device) != cudaSuccess) {
+        cudaGetLastError();
+        pageable = 0;
+    }
+    const char *hp = getenv("GBFFT_HOST_PATH");
+    ctx->host_direct = pageable == 1 && !(hp && !strcmp(hp, "staged"));
     if (const char *a = getenv("GBFFT_AUTOTUNE")) ctx->auto_tune = a[0] == '1';
     if (const char *a = getenv("GBFFT_AUTOTUNE_VERBOSE")) ctx->tune_verbose = a[0] == '1';
     *out_ctx = ctx.release();
@@ -584,6 +678,9 @@ void gbfft_destroy(gbfft_ctx *ctx) {
     ctx->ws.release();
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->hstage) cudaFreeHost(ctx->hstage);
+    if (ctx->htable) cudaFreeHost(ctx->htable);
+    ctx->dtable.release();
+    if (ctx->ev_table) cudaEventDestroy(ctx->ev_table);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -643,6 +740,8 @@ static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t
                            int direction) {
     const size_t row_bytes = (size_t)n * sizeof(float2);
     const bool pinned = host_is_pinned(in) && host_is_pinned(out);
+    if (!pinned && ctx->host_direct)
+        return host_pipeline_direct(ctx, n, batch, direction, (const char *)in, (char *)out, nullptr, nullptr);
     auto in_row = [&](uint64_t r) { return (const char *)in + r * row_bytes; };
     auto out_row = [&](uint64_t r) { return (char *)out + r * row_bytes; };
     return host_pipeline(ctx, n, batch, direction, pinned ? in : nullptr, pinned ? out : nullptr, in_row, out_row);
@@ -675,6 +774,7 @@ int gbfft_c2c_host_rows(gbfft_ctx *ctx, const float *const *in_rows, const uint6
     for (uint64_t i = 0; i < batch; ++i)
         if (!in_rows[i] || !out_rows[i]) return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "null row pointer");
     GB_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (ctx->host_direct) return host_pipeline_direct(ctx, n, batch, direction, nullptr, nullptr, in_rows, out_rows);
     auto in_row = [&](uint64_t r) { return (const char *)in_rows[r]; };
     auto out_row = [&](uint64_t r) { return (char *)out_rows[r]; };
     return host_pipeline(ctx, n, batch, direction, nullptr, nullptr, in_row, out_row);

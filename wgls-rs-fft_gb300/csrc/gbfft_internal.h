@@ -55,4 +55,13 @@ cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, 
                         const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
                         LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
 
+// ---- host rows <-> device batch, copied by the GPU (host_rows.cu) ---------
+// Moves `rows` rows of 2^logn complex<f32> between caller host memory, reached
+// through the host's page tables, and `dev` (the rows back to back).  Row r's
+// host address is table[r] (a device array) or, with table == nullptr,
+// base + r * 2^logn samples.  vec16: every host row address is 16-byte aligned
+// and logn >= 1.  Needs cudaDevAttrPageableMemoryAccess.
+cudaError_t host_rows_copy(const uint64_t *table, void *base, uint64_t rows, int logn, void *dev, bool to_device,
+                           bool vec16, int sms, cudaStream_t stream);
+
 }  // namespace gbfft

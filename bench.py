@@ -11,19 +11,30 @@ needed between steps.
 
   value      GSamples/s over the timed steps (CUDA events on the launching
              stream, max over ranks), samples counted per transform
-  e2e        same metric through the host C-ABI entry gbfft_c2c_host from
-             pinned host memory (H2D + transform + D2H inside the timed region)
+  e2e        same metric through the drop-in's host call gbfft_c2c_host_rows
+             over separately allocated pageable rows (the reference's
+             Vec<Vec<Complex<f32>>> argument), host<->device copies inside the
+             timed region; e2e_pinned: the contiguous entry gbfft_c2c_host
+             from pinned host buffers
   roofline   achieved HBM GB/s of the dominant kernel (16 bytes per sample
              per launch: one complex64 read + one write) vs the measured copy
              bandwidth
   cpu_baseline  the reference's Stockham R4/R2 path restated in C (the
              oracle), all host threads, on a bounded sample of the workload
+  extras     (default workload, one GPU) sub-records for the other targets,
+             each CUDA-event timed here with its own roofline and accuracy:
+             large_n (N = 2^24 x 4), split_vs_fp32 (N = 2^16 x 4096 tones,
+             every split kind against the FP32 form), ragged_vs_uniform (the
+             10,000-transform set), latency_rows (batch-1 latency of the
+             row entry, N = 256 .. 262144)
 
---impl reference times that CPU restatement alone on the same config.
+--impl reference times that CPU restatement alone on the same config (the
+whole batch every step).
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -247,6 +258,7 @@ def run_reference_arm(args, workload):
     if rank != 0:
         return 0
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
     import oracle
     import gbfft
     from gbfft import signals
@@ -254,36 +266,39 @@ def run_reference_arm(args, workload):
     threads = os.cpu_count() or 1
     what = "reference Stockham R4/R2 f32 path restated in C"
     if workload == "ragged_c5":
-        # a bounded sample of the ragged set: its transforms in descriptor order up
-        # to 2^22 samples a step, each (size, direction) group run as one batch
+        # the whole ragged set every step (the same seeded transforms the GPU arm
+        # runs), each (size, direction) group run as one batch
         descs, total = signals.ragged_set(args.ragged_count, seed=5)
-        groups, samples, count = {}, 0, 0
-        for L, d in zip(descs["log2n"].tolist(), descs["direction"].tolist()):
-            if samples >= (1 << 22):
-                break
-            groups[(L, d)] = groups.get((L, d), 0) + 1
-            samples += 1 << L
-            count += 1
-        jobs = [(signals.uniform_c64(b, 1 << L, seed=5 + L), d == gbfft.INVERSE) for (L, d), b in sorted(groups.items())]
+        x_all = signals.uniform_c64(1, total, seed=5)[0]
+        groups = {}
+        for off, L, d in descs.tolist():
+            groups.setdefault((L, d), []).append(off)
+        jobs = [(np.stack([x_all[o:o + (1 << L)] for o in offs]), d == gbfft.INVERSE)
+                for (L, d), offs in sorted(groups.items())]
+        del x_all
+        samples, count = total, len(descs)
 
         def step():
             for x, inv in jobs:
                 oracle.ref_fft(x, inv, threads)
-        sample = f"the first {count} of {len(descs)} transforms ({samples} samples) per step, {what}, {threads} threads"
+        sample = f"all {count} transforms ({samples} samples) per step, {what}, {threads} threads"
         data = "synthetic (seeded PCG hash, re/im iid U[-1,1))"
         config = {"workload": workload, "transforms": len(descs), "log2n": "uniform 8..18", "directions": "50/50",
                   "total_samples": total, "l2": "n/a (host)"}
     else:
         logn, batch, dist, seed = WORKLOADS[workload]
         n = 1 << logn
-        rows = max(threads, min(batch, 256 if n <= 4096 else max(1, (1 << 20) // n)))
+        # the whole batch when a step stays under 2^29 samples (about half a
+        # second on 16 cores); larger configurations run a bounded row sample
+        rows = batch if 2 * batch * n <= (1 << 29) else max(min(batch, threads), (1 << 28) // n)
         gen = {"normal": signals.normal_c64, "uniform": signals.uniform_c64, "tones": signals.tones_c64}[dist]
         x = gen(rows, n, seed=seed)
 
         def step():
             oracle.ref_fft(oracle.ref_fft(x, False, threads), True, threads)
         samples = 2 * rows * n
-        sample = f"{rows} of {batch} rows of N={n} per step (forward + inverse), {what}, {threads} threads"
+        sample = (f"the whole batch ({rows} rows of N={n}) per step" if rows == batch else
+                  f"{rows} of {batch} rows of N={n} per step") + f" (forward + inverse), {what}, {threads} threads"
         data = "synthetic (seeded PCG hash, " + {"normal": "re/im iid N(0,1))", "uniform": "re/im iid U[-1,1))",
                                                  "tones": "64 tones 10^U[-3,3] + N(0,1e-2) noise)"}[dist]
         config = {"workload": workload, "n": n, "batch": batch, "direction": "forward+inverse", "l2": "n/a (host)"}
@@ -308,31 +323,28 @@ def run_reference_arm(args, workload):
     return 0
 
 
-def run_ragged(args, ctx, dev, rank, world):
-    """Ragged workload: 10,000 transforms, log2 N uniform on 8..18, 50/50
-    directions, re/im uniform[-1,1) (seed 5), packed back to back (~4 GB).
-    One step = one execution of the whole set (one persistent launch, CUDA
-    graph replay).  Also times the same transforms as uniform batches (one
-    launch per (size, direction), data regrouped by size) for comparison."""
+def ragged_measure(ctx, dev, count, steps, warmup, precision, world=1, sampler=None):
+    """The ragged workload: `count` transforms, log2 N uniform on 8..18, 50/50
+    directions, re/im uniform[-1,1) (seed 5), packed back to back (~4 GB for
+    10,000).  One step = one execution of the whole set (one persistent launch,
+    CUDA graph replay).  Also times the same transforms as uniform batches
+    (one launch per (size, direction), data regrouped by size).  Returns a dict
+    of the measured figures."""
     import torch
     import gbfft
     from gbfft import signals
-    descs, total = signals.ragged_set(args.ragged_count, seed=5)
+    descs, total = signals.ragged_set(count, seed=5)
     x = signals.uniform_c64_torch(1, total, seed=5, device=dev)[0]
     y = torch.empty_like(x)
-    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3,
-            "tc_tf32": gbfft.PREC_TC_TF32}[args.precision]
-    ctx.set_precision(prec)  # the plan takes the context's precision
+    ctx.set_precision(PRECISIONS[precision])  # the plan takes the context's precision
     plan = ctx.ragged_plan(descs)
     # the uniform comparison uses the split form where the ragged kernel does (its two-pass
     # items, N >= 2^15); the ragged kernel's single-pass groups stay FP32, so do these
     ctx_small = gbfft.Context(dev.index or 0)
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
-    sampler = ClockSampler(dev.index or 0)
-    sampler.start()
     t_busy = time.time()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plan.execute(x, y, total, use_graph=True, stream=sp)
     plan.wait(stream=sp)
     if world > 1:
@@ -342,17 +354,17 @@ def run_ragged(args, ctx, dev, rank, world):
     ev1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.nvtx.range_push("timed")
     ev0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         plan.execute(x, y, total, use_graph=True, stream=sp)
     ev1.record(stream)
     torch.cuda.nvtx.range_pop()
     plan.wait(stream=sp)
     launches = plan.launch_count() - l0
-    sampler.keep_busy(t_busy, lambda: plan.execute(x, y, total, use_graph=True, stream=sp),
-                      lambda: plan.wait(stream=sp))
-    sampler.stop()
+    if sampler is not None:
+        sampler.keep_busy(t_busy, lambda: plan.execute(x, y, total, use_graph=True, stream=sp),
+                          lambda: plan.wait(stream=sp))
     ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
-    value = total * args.steps * world / (ms * 1e-3) / 1e9
+    value = total * steps * world / (ms * 1e-3) / 1e9
 
     # uniform-batch comparison: same transforms regrouped by (size, direction)
     groups = {}
@@ -372,10 +384,10 @@ def run_ragged(args, ctx, dev, rank, world):
     def uniform_step():
         for p0, n, b, d in calls:
             (ctx if n >= (1 << 15) else ctx_small).c2c_device(xu[p0:], yu[p0:], n, b, d, stream=sp)
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
         uniform_step()
     torch.cuda.synchronize(dev)
-    usteps = max(3, min(args.steps, 50))
+    usteps = max(3, min(steps, 50))
     ev0.record(stream)
     for _ in range(usteps):
         uniform_step()
@@ -383,6 +395,7 @@ def run_ragged(args, ctx, dev, rank, world):
     torch.cuda.synchronize(dev)
     ums = ev0.elapsed_time(ev1)
     uvalue = total * usteps / (ums * 1e-3) / 1e9
+    del xu, yu
 
     # one transform of every size against a float64 FFT (checker only)
     plan.execute(x, y, total, use_graph=True, stream=sp)
@@ -400,36 +413,198 @@ def run_ragged(args, ctx, dev, rank, world):
 
     sv_pass = lambda L: 1 if L <= 14 else 2  # graded accounting: 1 pass up to 2^14
     alg_bytes = sum(16 * (1 << L) * sv_pass(L) for L in descs["log2n"].tolist())
-    achieved = alg_bytes / (ms * 1e-3 / args.steps) / 1e9
+    achieved = alg_bytes / (ms * 1e-3 / steps) / 1e9
     exec_bytes = sum(16 * (1 << L) * (1 if L <= 13 else 2) for L in descs["log2n"].tolist())
+    plan.close()
+    ctx_small.close()
+    ctx.set_precision(gbfft.PREC_FP32)
+    return {"descs": descs, "total": total, "ms": ms, "steps": steps, "value": value, "launches": launches,
+            "uniform_value": uvalue, "uniform_launches_per_step": len(calls), "ratio": value / uvalue,
+            "worst_rel_l2": worst, "sizes_checked": len(seen), "alg_bytes": alg_bytes, "exec_bytes": exec_bytes,
+            "achieved": achieved}
+
+
+def run_ragged(args, ctx, dev, rank, world):
+    """One JSON line for the ragged workload (see ragged_measure)."""
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    t_busy = time.time()
+    r = ragged_measure(ctx, dev, args.ragged_count, args.steps, args.warmup, args.precision, world, sampler)
+    sampler.stop()
     peak, peak_kind = peaks()
     if rank == 0:
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded PCG hash, re/im iid U[-1,1))",
-            "config": {"workload": "ragged_c5", "transforms": len(descs), "log2n": "uniform 8..18",
-                       "directions": "50/50", "total_samples": total, "precision": args.precision,
+            "config": {"workload": "ragged_c5", "transforms": len(r["descs"]), "log2n": "uniform 8..18",
+                       "directions": "50/50", "total_samples": r["total"], "precision": args.precision,
                        "form": f"{args.precision} ragged persistent (graph)",
                        "l2": "inputs (4 GB) larger than L2; no flush", "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
+            "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": peak, "unit": "GB/s",
+                         "frac": r["achieved"] / peak,
                          "traffic": profile_traffic("ragged_c5", args.precision) if args.ragged_count == 10000 else None,
                          "peak_source": peak_kind,
-                         "alg_bytes_per_launch": alg_bytes, "executed_bytes_per_launch": exec_bytes,
-                         "launch_us": ms * 1e3 / max(1, launches)},
-            "uniform_batches": {"value": uvalue, "unit": UNIT, "launches_per_step": len(calls),
-                                "ragged_over_uniform": value / uvalue},
-            "cpu_baseline": None, "e2e": None, "gpu_launches": launches,
+                         "alg_bytes_per_launch": r["alg_bytes"], "executed_bytes_per_launch": r["exec_bytes"],
+                         "launch_us": r["ms"] * 1e3 / max(1, r["launches"])},
+            "uniform_batches": {"value": r["uniform_value"], "unit": UNIT,
+                                "launches_per_step": r["uniform_launches_per_step"],
+                                "ragged_over_uniform": r["ratio"]},
+            "cpu_baseline": None, "e2e": None, "gpu_launches": r["launches"],
             "clocks": sampler.summary(t_busy),
-            "accuracy": {"precision": args.precision, "max_rel_l2_vs_fp64": worst, "sizes_checked": len(seen),
+            "accuracy": {"precision": args.precision, "max_rel_l2_vs_fp64": r["worst_rel_l2"],
+                         "sizes_checked": r["sizes_checked"],
                          "reference": "float64 torch.fft of one transform per size (checker only)"},
         }
         print(json.dumps(line), flush=True)
-    plan.close()
-    ctx_small.close()
     return 0
+
+
+PRECISIONS = {"fp32": 0, "tc_fp16": 1, "tc_bf16x3": 2, "tc_tf32": 3}
+
+
+def time_pairs(ctx, x, y, z, n, batch, steps, warmup, stream, dev, world=1):
+    """Forward x -> y then inverse y -> z, `warmup` untimed and `steps` timed
+    pairs, CUDA events on `stream`; returns (ms over the timed pairs, max over
+    ranks; kernel launches in them)."""
+    import torch
+    import gbfft
+    sp = stream.cuda_stream
+    for _ in range(warmup):
+        ctx.c2c_device(x, y, n, batch, gbfft.FORWARD, stream=sp)
+        ctx.c2c_device(y, z, n, batch, gbfft.INVERSE, stream=sp)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    l0 = ctx.launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        ctx.c2c_device(x, y, n, batch, gbfft.FORWARD, stream=sp)
+        ctx.c2c_device(y, z, n, batch, gbfft.INVERSE, stream=sp)
+    ev1.record(stream)
+    torch.cuda.synchronize(dev)
+    return max_over_ranks(ev0.elapsed_time(ev1), dev), ctx.launch_count() - l0
+
+
+def rel_rows(y, x, rows, inverse=False):
+    """rel-L2 of y[rows] against a float64 FFT of x[rows] (checker only)."""
+    import torch
+    xr = x[rows].to(torch.complex128)
+    ref = torch.fft.ifft(xr, dim=1) if inverse else torch.fft.fft(xr, dim=1)
+    return (torch.linalg.vector_norm(y[rows].to(torch.complex128) - ref) / torch.linalg.vector_norm(ref)).item()
+
+
+def extra_large_n(ctx, dev, steps, warmup):
+    """N = 2^24 x 4 (512 MB), N(0,1), seed 3: the large-N target (>= 0.60 of
+    the HBM roofline under the graded two-pass accounting)."""
+    import torch
+    logn, batch = 24, 4
+    n = 1 << logn
+    x = make_input(logn, batch, "normal", 3, dev)
+    y, z = torch.empty_like(x), torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    ms, launches = time_pairs(ctx, x, y, z, n, batch, steps, warmup, stream, dev)
+    samples = 2 * n * batch * steps
+    value = samples / (ms * 1e-3) / 1e9
+    peak, kind = peaks()
+    achieved = value * 16 * 2  # GB/s: 16 bytes per sample per pass, 2 passes (graded)
+    acc = rel_rows(y, x, [0])
+    return {"workload": "n16777216_b4", "value": value, "unit": UNIT, "steps": steps,
+            "launches_per_transform": launches / (2 * steps),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": kind, "accounting": "16 B/sample x 2 passes per transform",
+                         "target_frac": 0.60, "meets_target": achieved / peak >= 0.60},
+            "accuracy": {"rel_l2_vs_fp64": acc, "rows": [0], "reference": "float64 torch.fft (checker only)"}}
+
+
+def extra_split_vs_fp32(ctx, dev, steps, warmup):
+    """N = 2^16 x 4096 tones workload (2^28 samples, 2 GB) in the FP32 form and
+    each split tensor-core kind: GSa/s, ratio to FP32, rel-L2 of sampled rows
+    against float64.  Target: a split kind at >= 1.2x FP32 with rel-L2 <= 2e-6."""
+    import torch
+    logn, batch = 16, 4096
+    n = 1 << logn
+    x = make_input(logn, batch, "tones", 4, dev, ctx)
+    y, z = torch.empty_like(x), torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+    rows = [0, 1365, 2730, 4095]
+    out = {"workload": "tones_n65536_b4096", "unit": UNIT, "steps": steps, "kinds": {}}
+    for name in ("fp32", "tc_fp16", "tc_tf32", "tc_bf16x3"):
+        ctx.set_precision(PRECISIONS[name])
+        ms, _ = time_pairs(ctx, x, y, z, n, batch, steps, warmup, stream, dev)
+        value = 2 * n * batch * steps / (ms * 1e-3) / 1e9
+        out["kinds"][name] = {"value": value, "rel_l2_vs_fp64": rel_rows(y, x, rows)}
+    ctx.set_precision(PRECISIONS["fp32"])
+    f = out["kinds"]["fp32"]["value"]
+    best = 0.0
+    for name, k in out["kinds"].items():
+        k["ratio_vs_fp32"] = k["value"] / f
+        k["within_2e-6"] = k["rel_l2_vs_fp64"] <= 2e-6
+        if name != "fp32" and k["within_2e-6"]:
+            best = max(best, k["ratio_vs_fp32"])
+    out.update({"best_split_ratio_within_2e-6": best, "target_ratio": 1.2, "meets_target": best >= 1.2,
+                "accuracy_rows": rows, "reference": "float64 torch.fft of the sampled rows (checker only)"})
+    return out
+
+
+def extra_ragged_vs_uniform(ctx, dev, steps, warmup):
+    r = ragged_measure(ctx, dev, 10000, steps, warmup, "fp32")
+    peak, kind = peaks()
+    return {"workload": "ragged_c5", "transforms": len(r["descs"]), "value": r["value"], "unit": UNIT,
+            "steps": steps, "launches_per_step": r["launches"] / steps,
+            "uniform_value": r["uniform_value"], "uniform_launches_per_step": r["uniform_launches_per_step"],
+            "ragged_over_uniform": r["ratio"], "target_ratio": 0.85, "meets_target": r["ratio"] >= 0.85,
+            "roofline": {"bound": "hbm", "achieved": r["achieved"], "peak": peak, "unit": "GB/s",
+                         "frac": r["achieved"] / peak, "peak_source": kind,
+                         "accounting": "16 B/sample x P(N) passes (1 up to 2^14, 2 above)"},
+            "accuracy": {"max_rel_l2_vs_fp64": r["worst_rel_l2"], "sizes_checked": r["sizes_checked"],
+                         "reference": "float64 torch.fft of one transform per size (checker only)"}}
+
+
+# The reference's published single-transform latency of GpuFft::fft, wall clock
+# with the host copies, on an unspecified NVIDIA GPU through wgpu/Vulkan
+# (README.md:107-118); shown beside ours for context only.
+REFERENCE_README_LATENCY_MS = {256: 0.095, 1024: 0.107, 4096: 0.128, 16384: 0.190, 65536: 0.452, 262144: 1.632}
+
+
+def rows_call(ctx, rows_in, rows_out, direction):
+    """One gbfft_c2c_host_rows call over separately allocated host rows, with
+    the pointer and length arrays built beforehand (as a Rust caller's
+    &[Vec<Complex<f32>>] gives them)."""
+    L = ctx._L
+    b = len(rows_in)
+    vp = ctypes.c_void_p
+    inp = (vp * b)(*[r.ctypes.data for r in rows_in])
+    outp = (vp * b)(*[r.ctypes.data for r in rows_out])
+    lens = (ctypes.c_uint64 * b)(*([rows_in[0].size] * b))
+    return lambda: ctx._check(L.gbfft_c2c_host_rows(ctx.handle, inp, lens, outp, b, direction))
+
+
+def extra_latency(ctx, reps=30):
+    """Batch-1 latency of the drop-in row entry (one row of N, pageable host
+    memory, copies both ways inside), median of `reps` calls."""
+    import numpy as np
+    import gbfft
+    from gbfft import signals
+    out = {"api": "gbfft_c2c_host_rows, one pageable row, forward", "reps": reps, "points": []}
+    for n, ref_ms in REFERENCE_README_LATENCY_MS.items():
+        r_in = [np.ascontiguousarray(signals.uniform_c64(1, n, seed=1)[0])]
+        r_out = [np.zeros_like(r_in[0])]
+        call = rows_call(ctx, r_in, r_out, gbfft.FORWARD)
+        for _ in range(5):
+            call()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            call()
+            ts.append(time.perf_counter() - t0)
+        ms = statistics.median(ts) * 1e3
+        out["points"].append({"n": n, "ms": ms, "msamples_per_s": n / ms * 1e-3,
+                              "reference_readme_ms": ref_ms})
+    return out
 
 
 def main():
@@ -439,7 +614,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ragged_c5"], default=DEFAULT_WORKLOAD)
-    ap.add_argument("--precision", choices=["fp32", "tc_fp16", "tc_bf16x3", "tc_tf32"], default="fp32")
+    ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
     ap.add_argument("--window", choices=["none", "hann"], default="none",
                     help="Hann window fused into every transform's load")
     ap.add_argument("--e2e-steps", type=int, default=10)
@@ -448,6 +623,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cufft", action="store_true", help="skip the reported cuFFT comparison")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the sub-records (large N, split vs FP32, ragged vs uniform, batch-1 latency)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -456,6 +633,7 @@ def main():
     if args.impl == "reference":
         return run_reference_arm(args, workload)
 
+    import numpy as np
     import torch
     import gbfft
 
@@ -475,9 +653,7 @@ def main():
     logn, batch, distn, seed = WORKLOADS[workload]
     n = 1 << logn
     x = make_input(logn, batch, distn, seed, dev, ctx)
-    prec = {"fp32": gbfft.PREC_FP32, "tc_fp16": gbfft.PREC_TC_FP16, "tc_bf16x3": gbfft.PREC_TC_BF16X3,
-            "tc_tf32": gbfft.PREC_TC_TF32}[args.precision]
-    ctx.set_precision(prec)
+    ctx.set_precision(PRECISIONS[args.precision])
     ctx.set_window(gbfft.WINDOW_HANN if args.window == "hann" else gbfft.WINDOW_NONE)
     y = torch.empty_like(x)
     z = torch.empty_like(x)
@@ -542,6 +718,7 @@ def main():
         rt = None              # both directions load through the window: no roundtrip identity
     ref64 = torch.fft.fft(xr, dim=1)
     acc = (torch.linalg.vector_norm(y[acc_rows].to(torch.complex128) - ref64) / torch.linalg.vector_norm(ref64)).item()
+    del xr, ref64
 
     # Reported GPU baseline: cuFFT (through torch.fft, batched C2C) on the same
     # device batch, forward + inverse per step.  A library call, timed the same
@@ -560,10 +737,40 @@ def main():
         cms = ev0.elapsed_time(ev1)
         cufft = {"value": samples_per_step * csteps / (cms * 1e-3) / 1e9, "unit": UNIT, "steps": csteps,
                  "api": "torch.fft.fft/ifft (cuFFT), out of place"}
+        torch.cuda.empty_cache()
 
-    # end to end through the host C ABI from pinned memory
-    e2e = None
+    # End to end through the drop-in's own call: gbfft_c2c_host_rows over
+    # `batch` separately allocated pageable host rows (the reference's
+    # &[Vec<Complex<f32>>] argument shape, src/lib.rs:433-438, 517-568),
+    # forward then inverse each step, host -> device and device -> host copies
+    # inside the timed region.  Beside it the contiguous entry from pinned
+    # host buffers (gbfft_c2c_host).
+    e2e = e2e_pinned = None
     if not args.no_e2e:
+        xh = x.cpu().numpy()
+        rows_x = [np.array(r) for r in xh]          # one allocation per row
+        rows_y = [np.zeros_like(r) for r in rows_x]
+        rows_z = [np.zeros_like(r) for r in rows_x]
+        fwd = rows_call(ctx, rows_x, rows_y, gbfft.FORWARD)
+        inv = rows_call(ctx, rows_y, rows_z, gbfft.INVERSE)
+        fwd()
+        inv()
+        if world > 1:
+            torch.distributed.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            fwd()
+            inv()
+        el = max_over_ranks(time.perf_counter() - t0, dev)
+        nbytes = 8 * n * batch
+        chk = rows_z[batch // 2]
+        e2e = {"value": samples_per_step * args.e2e_steps * world / el / 1e9, "unit": UNIT,
+               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
+               "steps": args.e2e_steps,
+               "api": f"gbfft_c2c_host_rows ({batch} separately allocated pageable rows of {n}, "
+                      "the reference's Vec<Vec<Complex<f32>>> shape)",
+               "roundtrip_rel_l2_row": float(np.linalg.norm(chk - xh[batch // 2]) / np.linalg.norm(xh[batch // 2]))}
+        del rows_x, rows_y, rows_z
         hx = x.cpu().pin_memory()
         hy = torch.empty_like(hx).pin_memory()
         hz = torch.empty_like(hx).pin_memory()
@@ -576,10 +783,10 @@ def main():
             ctx.c2c_host_ptr(hx.data_ptr(), hy.data_ptr(), n, batch, gbfft.FORWARD)
             ctx.c2c_host_ptr(hy.data_ptr(), hz.data_ptr(), n, batch, gbfft.INVERSE)
         el = max_over_ranks(time.perf_counter() - t0, dev)
-        nbytes = 8 * n * batch
-        e2e = {"value": samples_per_step * args.e2e_steps * world / el / 1e9, "unit": UNIT,
-               "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
-               "steps": args.e2e_steps, "api": "gbfft_c2c_host (pinned host buffers)"}
+        e2e_pinned = {"value": samples_per_step * args.e2e_steps * world / el / 1e9, "unit": UNIT,
+                      "h2d_bytes_per_step": 2 * nbytes, "d2h_bytes_per_step": 2 * nbytes,
+                      "steps": args.e2e_steps, "api": "gbfft_c2c_host (pinned contiguous host buffers)"}
+        del hx, hy, hz
 
     cpu = cpu_lib = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -594,6 +801,23 @@ def main():
             cpu_lib = {"value": lib[0], "unit": UNIT, "cores": threads,
                        "library": "scipy.fft (pocketfft) complex64, workers=-1",
                        "sample": f"{lib[1]} of {batch} rows of N={n}, forward+inverse, repeated {lib[2]}x"}
+
+    # Sub-records for the other targets, each timed in this process with CUDA
+    # events and carrying its own roofline and accuracy (one GPU only).
+    extras = None
+    if not args.no_extras and world == 1 and workload == DEFAULT_WORKLOAD and args.precision == "fp32" \
+            and args.window == "none":
+        del y, z
+        torch.cuda.empty_cache()
+        esteps = max(3, min(args.steps, 20))
+        extras = {}
+        extras["large_n"] = extra_large_n(ctx, dev, esteps, 3)
+        torch.cuda.empty_cache()
+        extras["split_vs_fp32"] = extra_split_vs_fp32(ctx, dev, max(3, min(args.steps, 10)), 3)
+        torch.cuda.empty_cache()
+        extras["ragged_vs_uniform"] = extra_ragged_vs_uniform(ctx, dev, max(3, min(args.steps, 10)), 3)
+        torch.cuda.empty_cache()
+        extras["latency_rows"] = extra_latency(ctx)
 
     if rank == 0:
         line = {
@@ -622,11 +846,13 @@ def main():
             "cufft_baseline": cufft,
             "gflops": value * 5 * logn,  # 5 N log2 N flops per transform (the reference's model)
             "e2e": e2e,
+            "e2e_pinned": e2e_pinned,
             "gpu_launches": launches,
             "clocks": sampler.summary(t_busy),
             "roundtrip_rel_l2": rt,
             "accuracy": {"precision": args.precision, "rel_l2_vs_fp64": acc, "rows": acc_rows,
                          "reference": "float64 torch.fft of the sampled rows (checker only)"},
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -91,8 +91,10 @@ def test_parse_ncu_csv_aggregates_per_kernel(lib_built):
 
 
 def test_ncu_counters_runs_plain_first_then_ncu(lib_built, tmp_path):
-    """The capture runs only after the same child command exited 0 without
-    ncu; a failing plain run raises before ncu is started."""
+    """The captures run only after the same child command exited 0 without
+    ncu; a failing plain run raises before ncu is started.  The first capture
+    is a launch list with device time only; DRAM counters are then collected
+    for the dominant kernel alone, one launch."""
     from gbfft import leaderboard as lb
     calls = []
 
@@ -110,8 +112,12 @@ def test_ncu_counters_runs_plain_first_then_ncu(lib_built, tmp_path):
         return R(0)
 
     ks = lb.ncu_counters(1024, 0, run=fake_run)
-    assert len(calls) == 2 and calls[0][0] != "ncu" and calls[1][0] == "ncu"
-    assert calls[1][calls[1].index("--metrics") + 1] == ",".join(lb.NCU_METRICS)
-    assert ks[0].launches == 2
+    assert len(calls) == 3 and calls[0][0] != "ncu" and calls[1][0] == "ncu" and calls[2][0] == "ncu"
+    assert calls[1][calls[1].index("--metrics") + 1] == "gpu__time_duration.sum"
+    assert "-k" not in calls[1] and "-c" not in calls[1]
+    assert calls[2][calls[2].index("--metrics") + 1] == "dram__bytes_read.sum,dram__bytes_write.sum"
+    assert calls[2][calls[2].index("-k") + 1] == "regex:fft_rows_kernel" and calls[2][calls[2].index("-c") + 1] == "1"
+    assert ks[0].launches == 2 and ks[0].dram_bytes == 4 * 8388608  # two launches of 2 x 8 MB (fake data)
+    assert ks[1].dram_bytes != ks[1].dram_bytes  # nan: not captured
     with pytest.raises(RuntimeError):
         lb.ncu_counters(1024, 0, run=lambda cmd, **kw: R(1))

@@ -2,7 +2,7 @@
 examples/rivalry_leaderboard.rs), with the GB300 executor registered.
 
 For each N in {256, 1024, 16384, 65536, 2^20} and the reference's batch rule
-(choose_batch_size, examples/rivalry_leaderboard.rs:147-166, capped at
+(choose_batch_size, examples/rivalry_leaderboard.rs:159-177, capped at
 MAX_TOTAL_SAMPLES = 16 Mi samples, src/benchmark.rs:47), every rival's
 host-vector ``fft`` -- the complete pipeline: host to device, transform,
 device to host -- is run 3 times untimed and 10 times timed
@@ -22,11 +22,13 @@ Rivals:
     src/cufft_wrapper.rs:49-54)
 
 With --ncu, each size is followed by the device-side counters of the GB300
-rivals: the rival's transform of the same batch is run once plainly and then
-once under Nsight Compute (launch-list metrics only: device time and DRAM
-bytes of every kernel inside an NVTX range), and each kernel's launches, time,
-DRAM traffic and achieved DRAM bandwidth are printed beside the algorithmic
-traffic (16 bytes per sample per pass, 1 pass up to N = 2^14, 2 above).
+rivals: the rival's transform of the same batch is run once plainly, then
+under Nsight Compute twice -- a launch list (device time only, one pass, every
+kernel inside an NVTX range), then the DRAM bytes of the dominant kernel
+alone (its first launch in the range) -- and each kernel's launches and time,
+and the dominant kernel's DRAM traffic and achieved DRAM bandwidth, are
+printed beside the algorithmic traffic (16 bytes per sample per pass, 1 pass
+up to N = 2^14, 2 above).
 
 Run:  python -m gbfft.leaderboard [--sizes 256 1024 ...] [--ncu]
 """
@@ -57,7 +59,7 @@ FFT_SIZES = (256, 1024, 16384, 65536, 1048576)
 
 
 def choose_batch_size(n: int) -> int:
-    """examples/rivalry_leaderboard.rs:147-166"""
+    """examples/rivalry_leaderboard.rs:159-177"""
     if n <= 1024:
         batch = 1024
     elif n <= 16384:
@@ -188,6 +190,8 @@ def format_table(n: int, results: Sequence[Result]) -> str:
 # ---- device-side counters (Nsight Compute) ---------------------------------
 
 NCU_METRICS = ("gpu__time_duration.sum", "dram__bytes_read.sum", "dram__bytes_write.sum")
+NCU_TIME_METRICS = NCU_METRICS[:1]   # launch list: every kernel in the range
+NCU_DRAM_METRICS = NCU_METRICS[1:]   # the dominant kernel only, one launch
 NCU_RANGE = "gbfft_measure"
 
 
@@ -247,9 +251,20 @@ def ncu_child(n: int, precision: int) -> int:
     return 0
 
 
+def _kernel_regex(short: str) -> str:
+    """ncu -k filter on a kernel's function name without namespace or
+    template arguments: 'gbfft::fft_rows_kernel<10, 11>' -> 'regex:fft_rows_kernel'."""
+    import re
+    base = short.split("<")[0].split("::")[-1].strip()
+    return "regex:" + re.escape(base)
+
+
 def ncu_counters(n: int, precision: int, ncu: str = "ncu", run=subprocess.run) -> List[KernelCounters]:
     """Run the size's transform plainly, then (only if that exited 0) under
-    ncu with the launch-list metrics, and return the per-kernel counters."""
+    ncu: first a launch list with device time only (one pass per launch), then
+    the DRAM read/write bytes of the dominant kernel alone, one launch
+    (-k <its name> -c 1).  The dominant kernel's DRAM bytes are that launch's
+    times its launch count; the other kernels carry no DRAM figure (nan)."""
     child = [sys.executable, "-m", "gbfft.leaderboard", "--ncu-child", str(n), "--precision", str(precision)]
     env = dict(os.environ)
     pkg_parent = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -259,13 +274,30 @@ def ncu_counters(n: int, precision: int, ncu: str = "ncu", run=subprocess.run) -
         raise RuntimeError(f"plain run failed ({plain.returncode}): {plain.stderr[-400:]}")
     with tempfile.TemporaryDirectory() as d:
         log = os.path.join(d, "launches.csv")
-        cmd = [ncu, "--metrics", ",".join(NCU_METRICS), "--clock-control", "none", "--nvtx", "--nvtx-include",
+        cmd = [ncu, "--metrics", ",".join(NCU_TIME_METRICS), "--clock-control", "none", "--nvtx", "--nvtx-include",
                f"{NCU_RANGE}/", "--print-units", "base", "--csv", "--log-file", log, *child]
         r = run(cmd, env=env, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"ncu failed ({r.returncode}): {r.stderr[-400:]}")
         with open(log) as f:
-            return parse_ncu_csv(f.read())
+            counters = parse_ncu_csv(f.read())
+        if not counters:
+            return counters
+        for k in counters:
+            k.dram_bytes = float("nan")
+        top = counters[0]
+        log2 = os.path.join(d, "dram.csv")
+        cmd = [ncu, "--metrics", ",".join(NCU_DRAM_METRICS), "--clock-control", "none", "--nvtx", "--nvtx-include",
+               f"{NCU_RANGE}/", "-k", _kernel_regex(top.kernel), "-c", "1", "--print-units", "base", "--csv",
+               "--log-file", log2, *child]
+        r = run(cmd, env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"ncu failed ({r.returncode}): {r.stderr[-400:]}")
+        with open(log2) as f:
+            one = parse_ncu_csv(f.read())
+        if one and one[0].launches:
+            top.dram_bytes = one[0].dram_bytes / one[0].launches * top.launches
+        return counters
 
 
 def format_counters(n: int, batch: int, label: str, counters: Sequence[KernelCounters]) -> str:
@@ -276,6 +308,9 @@ def format_counters(n: int, batch: int, label: str, counters: Sequence[KernelCou
              f"algorithmic traffic {alg / 1e6:.1f} MB ({passes} pass(es) x 16 B/sample) = "
              f"{(alg / total_t / 1e9) if total_t > 0 else float('nan'):.0f} GB/s"]
     for k in counters:
+        if math.isnan(k.dram_bytes):
+            lines.append(f"    {k.kernel:<48} x{k.launches:<3} {k.seconds * 1e6:>10.1f} us")
+            continue
         bw = k.dram_bytes / k.seconds / 1e9 if k.seconds > 0 else float("nan")
         lines.append(f"    {k.kernel:<48} x{k.launches:<3} {k.seconds * 1e6:>10.1f} us  DRAM {k.dram_bytes / 1e6:>9.1f} MB"
                      f"  {bw:>7.0f} GB/s")

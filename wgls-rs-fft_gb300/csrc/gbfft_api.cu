@@ -116,6 +116,7 @@ struct gbfft_ctx {
     // on different streams never share one
     std::map<cudaStream_t, std::unique_ptr<DeviceBuffer>> fused_ctr;
     uint32_t *d_err = nullptr;  // raised by tensor-core and fused kernels when a bounded wait gives up
+    bool err_armed = false;     // a kernel that can raise d_err was enqueued since it was last read
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
     uint64_t launches = 0;
@@ -219,6 +220,8 @@ int get_plan(gbfft_ctx *ctx, int logn, const PlanVariant &v, Plan **out) {
 
 // After a synchronisation: report (and clear) a device-side wait that gave up.
 int check_device_flag(gbfft_ctx *ctx) {
+    if (!ctx->err_armed) return GBFFT_OK;  // only FP32 kernels without waits ran: nothing can be raised
+    ctx->err_armed = false;
     uint32_t v = 0;
     GB_CUDA(ctx, cudaMemcpy(&v, ctx->d_err, sizeof v, cudaMemcpyDeviceToHost));
     if (v != 0) {
@@ -306,6 +309,7 @@ int run_variant(gbfft_ctx *ctx, const float2 *in, float2 *out, uint64_t n, uint6
         if (!b) b.reset(new DeviceBuffer());
         ctr = b.get();
     }
+    if (plan->has_fused || ctx->precision != GBFFT_PREC_FP32) ctx->err_armed = true;
     st = plan_execute(*plan, in, out, batch, direction, ctx->ws, ctx->d_err, stream, launches, why, ops, ctr);
     ctx->launches += launches;
     if (st != GBFFT_OK) return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n,
@@ -527,6 +531,11 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     char *dy = (char *)ctx->dbuf_out.ptr;
     const uint64_t *tin = nullptr, *tout = nullptr;
     uintptr_t align_bits = 0;
+    if (in_rows && batch == 1) {  // one row: its own address is the base, no pointer table
+        in_base = (const char *)in_rows[0];
+        out_base = (char *)out_rows[0];
+        in_rows = nullptr;
+    }
     if (in_rows) {
         const size_t tbytes = 2 * batch * sizeof(uint64_t);
         if (ctx->htable_bytes < tbytes) {
@@ -567,6 +576,7 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
         if (st != GBFFT_OK) return st;
         if (plan->passes.size() >= 3) rows_per_chunk = batch;
     }
+    const size_t nchunks = (batch + rows_per_chunk - 1) / rows_per_chunk;
     size_t c = 0;
     for (uint64_t r0 = 0; r0 < batch; r0 += rows_per_chunk, ++c) {
         const uint64_t rows = std::min(batch - r0, rows_per_chunk);
@@ -580,7 +590,7 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
                                     logn, dy + off, false, vec16, ctx->sms, s));
         ctx->launches += 2;
     }
-    for (auto &s : ctx->xfer) GB_CUDA(ctx, cudaStreamSynchronize(s));
+    for (size_t k = 0; k < std::min<size_t>(nchunks, 3); ++k) GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[k]));
     return check_device_flag(ctx);
 }
 

@@ -461,7 +461,7 @@ def run_ragged(args, ctx, dev, rank, world):
     return 0
 
 
-PRECISIONS = {"fp32": 0, "tc_fp16": 1, "tc_bf16x3": 2, "tc_tf32": 3}
+PRECISIONS = {"fp32": 0, "tc_fp16": 1, "tc_bf16x3": 2, "tc_tf32": 3, "tc_bf16x6": 4}
 
 
 def time_pairs(ctx, x, y, z, n, batch, steps, warmup, stream, dev, world=1):
@@ -532,7 +532,7 @@ def extra_split_vs_fp32(ctx, dev, steps, warmup):
     stream = torch.cuda.current_stream(dev)
     rows = [0, 1365, 2730, 4095]
     out = {"workload": "tones_n65536_b4096", "unit": UNIT, "steps": steps, "kinds": {}}
-    for name in ("fp32", "tc_fp16", "tc_tf32", "tc_bf16x3"):
+    for name in ("fp32", "tc_fp16", "tc_tf32", "tc_bf16x3", "tc_bf16x6"):
         ctx.set_precision(PRECISIONS[name])
         ms, _ = time_pairs(ctx, x, y, z, n, batch, steps, warmup, stream, dev)
         value = 2 * n * batch * steps / (ms * 1e-3) / 1e9

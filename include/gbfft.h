@@ -54,9 +54,12 @@ typedef enum gbfft_precision {
                                  (3 products), per-vector power-of-two scaling, FP32 accumulation;
                                  N >= 16 (TF32: single-pass sizes up to 2^13, then N >= 2^15) */
     GBFFT_PREC_TC_BF16X3 = 2, /* same with BF16 hi+lo operands */
-    GBFFT_PREC_TC_TF32 = 3    /* same with TF32 hi+lo operands (hi = the value rounded to TF32,
+    GBFFT_PREC_TC_TF32 = 3,   /* same with TF32 hi+lo operands (hi = the value rounded to TF32,
                                  lo = the exact rest); TF32 keeps FP32's exponent range, so no
                                  scaling */
+    GBFFT_PREC_TC_BF16X6 = 4  /* BF16 operands split in three (hi + mid + lo: 24 significant bits),
+                                 six products (hh, hm, mh, hl, lh, mm), no scaling: the BF16 form
+                                 inside the FP32 form's error budget */
 } gbfft_precision;
 
 typedef struct gbfft_ctx gbfft_ctx;
@@ -241,7 +244,7 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
 
 /* Environment read by the library:
  *   GBFFT_AUTOTUNE, GBFFT_AUTOTUNE_CACHE   see gbfft_autotune
- *   GBFFT_PRECISION=tc_fp16|tc_bf16x3|tc_tf32  default precision of new contexts
+ *   GBFFT_PRECISION=tc_fp16|tc_bf16x3|tc_tf32|tc_bf16x6  default precision of new contexts
  *   GBFFT_HOST_CHUNK_BYTES=<bytes>         chunk of the host-batch pipeline (32 MB)
  *   GBFFT_HOST_PATH=staged                 pageable host batches go through pinned
  *                                          staging even where the GPU could reach

@@ -257,7 +257,7 @@ def test_three_pass_persistent_first_pass(tmp_path, monkeypatch, oracle, lib_bui
     assert oracle.rel_l2(z, x) <= 1e-6
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (3, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (3, 2e-6), (4, 2e-6)])
 def test_autotune_split_form(tmp_path, monkeypatch, oracle, lib_built, prec, tol):
     """The tuner at a split precision times the split form's own candidates
     (fused pass pair, one launch per pass), caches the choice under that

@@ -13,8 +13,8 @@ on those same inputs:
       The reference path is no gate here: its f32 twiddle angles put it more
       than 1e-3 from FP64 on its own benchmark input above N = 2^20.
   C4  N = 2^16 x 4096 tones workload in the split tensor-core forms: sampled
-      rows against FP64 (2e-6 for FP16 and TF32 hi+lo, the FP32 form's own
-      budget), with the FP32 form on the same rows beside it.
+      rows against FP64 (2e-6 for FP16 and TF32 hi+lo and BF16 x 6, the FP32
+      form's own budget), with the FP32 form on the same rows beside it.
   C5  the seeded 10,000-transform ragged set (one persistent launch): up to
       64 transforms of every (size, direction) against the reference path
       (1e-3) and FP64 (2e-6).
@@ -81,11 +81,12 @@ def test_c3_default_plan_vs_fp64(gpu_ctx, oracle, torch, logn, batch, inv_rows):
     assert err <= TOL_REL_L2, err
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (3, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (3, 2e-6), (4, 2e-6)])
 def test_c4_full_size_split_forms_vs_fp64(lib_built, oracle, torch, prec, tol):
-    """N = 2^16 x 4096 (2^28 samples) in FP16 hi+lo (prec 1) and TF32 hi+lo
-    (prec 3): 64 rows spread over the batch against FP64, forward and
-    inverse, with the FP32 form on the same rows (both within the budget)."""
+    """N = 2^16 x 4096 (2^28 samples) in FP16 hi+lo (prec 1), TF32 hi+lo
+    (prec 3) and BF16 x 6 (prec 4): 64 rows spread over the batch against
+    FP64, forward and inverse, with the FP32 form on the same rows (both
+    within the budget)."""
     import gbfft
     from gbfft import signals
     n, batch = 1 << 16, 4096

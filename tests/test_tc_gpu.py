@@ -6,7 +6,9 @@ Gates, stated where used:
     gate as the FP32 form;
   * BF16x3 (16-bit significand pairs): its measured error is about 6e-6, so it
     is held to 2e-5 and reported, not claimed against the 2e-6 gate;
-  * both: max |a - b| <= 1e-3 against the reference path on the reference's
+  * BF16x6 (three BF16 parts, 24 significant bits, 6 products): 2e-6, the
+    FP32 form's own gate (prec 4);
+  * all: max |a - b| <= 1e-3 against the reference path on the reference's
     benchmark input (src/benchmark.rs:204-217, 272-297).
 """
 import numpy as np
@@ -23,7 +25,7 @@ def tc_ctx(lib_built):
     ctx.close()
 
 
-@pytest.mark.parametrize("prec", [1, 3])
+@pytest.mark.parametrize("prec", [1, 3, 4])
 @pytest.mark.parametrize("logn,batch", [(15, 4), (16, 8), (17, 2), (18, 3), (20, 1), (22, 1)])
 def test_tc_split_vs_fp64(tc_ctx, oracle, logn, batch, prec):
     import gbfft
@@ -36,7 +38,7 @@ def test_tc_split_vs_fp64(tc_ctx, oracle, logn, batch, prec):
         assert err <= 2e-6, (logn, inv, err)
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6), (4, 2e-6)])
 def test_tc_tones_workload(tc_ctx, oracle, prec, tol):
     """The split-form workload at reduced batch: 64 tones at seeded bins with
     amplitudes 10^U[-3,3] and phases U[0, 2 pi), plus N(0, 1e-2) noise."""
@@ -49,7 +51,7 @@ def test_tc_tones_workload(tc_ctx, oracle, prec, tol):
     assert err <= tol, err
 
 
-@pytest.mark.parametrize("prec", [1, 2, 3])
+@pytest.mark.parametrize("prec", [1, 2, 3, 4])
 def test_tc_reference_path_gate(tc_ctx, oracle, prec):
     import gbfft
     tc_ctx.set_precision(prec)
@@ -83,7 +85,7 @@ def test_tc_matches_fp32_form_and_limits(tc_ctx, oracle):
     tc_ctx.set_precision(gbfft.PREC_FP32)
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6), (4, 2e-6)])
 @pytest.mark.parametrize("logn,batch", [(15, 3), (16, 5), (17, 2), (18, 3)])
 def test_tc_fused_pair_matches_two_launches(lib_built, oracle, prec, tol, logn, batch):
     """Two-pass sizes out of place on the device run both passes in one
@@ -117,7 +119,7 @@ def test_tc_fused_pair_matches_two_launches(lib_built, oracle, prec, tol, logn, 
             assert oracle.rel_l2(fused, two) <= 1e-6
 
 
-@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6)])
+@pytest.mark.parametrize("prec,tol", [(1, 2e-6), (2, 2e-5), (3, 2e-6), (4, 2e-6)])
 @pytest.mark.parametrize("logn", list(range(4, 15)))
 def test_tc_single_pass_sizes(tc_ctx, oracle, prec, tol, logn):
     """The split form's single-pass kernel (N = 2^4 .. 2^14; TF32 up to 2^13):
@@ -182,3 +184,15 @@ def test_tc_radix32_fused_pair(lib_built, oracle, tmp_path, monkeypatch, prec, t
         assert err <= tol, (inv, err)
     for a, b in zip(outs[4], outs[5]):
         assert oracle.rel_l2(b, a) <= 2 * tol
+
+
+def test_precision_values(tc_ctx):
+    """Every precision of the header is accepted; anything else is refused."""
+    import gbfft
+    for p in (gbfft.PREC_FP32, gbfft.PREC_TC_FP16, gbfft.PREC_TC_BF16X3, gbfft.PREC_TC_TF32, gbfft.PREC_TC_BF16X6):
+        tc_ctx.set_precision(p)
+    for bad in (-1, 5, 99):
+        with pytest.raises(gbfft.GbfftError) as e:
+            tc_ctx.set_precision(bad)
+        assert e.value.status == gbfft.ERR_INVALID_ARGUMENT
+    tc_ctx.set_precision(gbfft.PREC_FP32)

@@ -38,19 +38,22 @@ constexpr int tc_groups() {
 }
 
 // Shared memory of a tensor-core tile kernel: the item region (FP32 exchange
-// tile + column twiddles; the hi/lo A operands alias it while a tensor-core
+// tile + column twiddles; the A operand parts alias it while a tensor-core
 // DFT runs -- every tc_dft16 waits for the tile's readers before writing A),
-// then the two G parts, then the mbarrier, TMEM address and abort flag.
+// then the G parts (two, three for BF16 x 6), then the mbarrier, TMEM address
+// and abort flag.
 template <int KIND, int THREADS, size_t TILE_BYTES, int RADIX = 16>
 struct TcSmem {
     using Gm = TcGeom<KIND, RADIX>;
+    static constexpr int RADIX_ = RADIX;
     static constexpr int NMMA = THREADS / 128;
     static_assert(THREADS % 128 == 0, "one M = 128 MMA per 128 threads");
     static constexpr uint32_t TMEM_COLS = tc_tmem_cols(NMMA * RADIX / 16);  // 2 RADIX columns per block
     static constexpr size_t A_BYTES = (size_t)THREADS * Gm::ROW_BYTES;
-    static constexpr size_t REGION = ((2 * A_BYTES > TILE_BYTES ? 2 * A_BYTES : TILE_BYTES) + 1023) & ~(size_t)1023;
+    static constexpr size_t A_ALL = Gm::PARTS * A_BYTES;
+    static constexpr size_t REGION = ((A_ALL > TILE_BYTES ? A_ALL : TILE_BYTES) + 1023) & ~(size_t)1023;
     static constexpr size_t OFF_G = REGION;
-    static constexpr size_t OFF_MISC = OFF_G + 2 * (size_t)Gm::G_BYTES;
+    static constexpr size_t OFF_MISC = OFF_G + Gm::PARTS * (size_t)Gm::G_BYTES;
     static constexpr size_t SMEM = OFF_MISC + 64;
     // CTAs per SM that shared memory allows (228 KB per SM, 1 KB reserved per CTA)
     static constexpr int FIT = (int)((228u * 1024u) / (SMEM + 1024u));
@@ -67,7 +70,7 @@ __device__ __forceinline__ void tc_cta_setup(uint8_t *smem, const uint4 *__restr
     const int tid = threadIdx.x;
     const uint4 *gsrc = gtab + Gm::GTAB_OFF / 16;
     uint4 *gdst = (uint4 *)(smem + L::OFF_G);
-    for (int i = tid; i < 2 * Gm::G_BYTES / 16; i += blockDim.x) gdst[i] = gsrc[i];
+    for (int i = tid; i < Gm::PARTS * Gm::G_BYTES / 16; i += blockDim.x) gdst[i] = gsrc[i];
     if (tid < 32) tmem_alloc(s_taddr, L::TMEM_COLS);
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -76,10 +79,7 @@ __device__ __forceinline__ void tc_cta_setup(uint8_t *smem, const uint4 *__restr
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    st.a_hi = smem;
-    st.a_lo = smem + L::A_BYTES;
-    st.g_hi = smem + L::OFF_G;
-    st.g_lo = smem + L::OFF_G + Gm::G_BYTES;
+    tc_state_parts<KIND, L::RADIX_>(st, smem, L::A_BYTES, smem + L::OFF_G);
     st.bar = bar;
     st.abort = s_abort;
     st.err = err;
@@ -214,6 +214,7 @@ bool pass_tc_kernel_info(int logr, bool first, int precision, PassDesc &d) {
     d.logr = logr;
     switch (tc_kind_of_precision(precision)) {
         case kTcBF16: return pass_tc_info_kind<kTcBF16>(logr, first, d);
+        case kTcBF16X6: return pass_tc_info_kind<kTcBF16X6>(logr, first, d);
         case kTcTF32: return pass_tc_info_kind<kTcTF32>(logr, first, d);
         default: return pass_tc_info_kind<kTcF16>(logr, first, d);
     }
@@ -256,7 +257,7 @@ static void fused_tc_describe(FusedDesc &d) {
 template <int KIND>
 static bool fused_tc_info_kind(int logr1, int logr2, FusedDesc &d, int loge) {
     if (loge == 5) {
-        if constexpr (KIND == kTcTF32) {
+        if constexpr (KIND == kTcTF32 || KIND == kTcBF16X6) {
             return false;
         } else {
 #define GBFFT_FTC5(A, B) \
@@ -283,6 +284,7 @@ static bool fused_tc_info_kind(int logr1, int logr2, FusedDesc &d, int loge) {
 bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d, int loge) {
     switch (tc_kind_of_precision(precision)) {
         case kTcBF16: return fused_tc_info_kind<kTcBF16>(logr1, logr2, d, loge);
+        case kTcBF16X6: return fused_tc_info_kind<kTcBF16X6>(logr1, logr2, d, loge);
         case kTcTF32: return fused_tc_info_kind<kTcTF32>(logr1, logr2, d, loge);
         default: return fused_tc_info_kind<kTcF16>(logr1, logr2, d, loge);
     }
@@ -292,7 +294,9 @@ bool fused_tc_kernel_info(int logr1, int logr2, int precision, FusedDesc &d, int
 // out = [fp16 hi | fp16 lo | bf16 hi | bf16 lo] (2048 bytes each), then
 // [tf32 hi | tf32 lo] (4096 bytes each).  The TF32 parts come from the FP64
 // value: hi = the FP32 value with its 13 low mantissa bits cleared, lo = the
-// rest rounded to the nearest TF32 value.
+// rest rounded to the nearest TF32 value.  The three BF16 parts of the BF16 x 6
+// kind, [hi | lo | mid] (2048 bytes each), follow the radix-32 parts at byte
+// 49152: hi = RN(g), mid = RN(g - hi), lo = RN(g - hi - mid), from the FP64 g.
 __global__ void tc_gtab_kernel(uint8_t *out) {
     const int i = threadIdx.x + blockIdx.x * blockDim.x;
     if (i >= 32 * 32) return;
@@ -319,6 +323,14 @@ __global__ void tc_gtab_kernel(uint8_t *out) {
     const uint32_t off32 = TcGeom<kTcTF32>::elem_offset(n, k);
     *(uint32_t *)(out + 8192 + off32) = th;
     *(uint32_t *)(out + 8192 + 4096 + off32) = tl;
+    const __nv_bfloat16 x6h = __double2bfloat16(g);
+    const double r1 = g - (double)__bfloat162float(x6h);
+    const __nv_bfloat16 x6m = __double2bfloat16(r1);
+    const __nv_bfloat16 x6l = __double2bfloat16(r1 - (double)__bfloat162float(x6m));
+    uint8_t *x6 = out + TcGeom<kTcBF16X6>::GTAB_OFF;
+    *(uint16_t *)(x6 + 0 * 2048 + off) = __bfloat16_as_ushort(x6h);
+    *(uint16_t *)(x6 + 1 * 2048 + off) = __bfloat16_as_ushort(x6l);
+    *(uint16_t *)(x6 + 2 * 2048 + off) = __bfloat16_as_ushort(x6m);
 }
 
 // Radix-32 G (64 x 64) parts for the 32-sample tiles, after the radix-16 ones:

@@ -236,13 +236,13 @@ fft_ragged_tc_kernel(RagParams P, const uint4 *__restrict__ gtab, uint32_t off_g
     using Lay = RagTcLayout<KIND>;
     using Gm = TcGeom<KIND>;
     extern __shared__ __align__(1024) uint8_t smem_rtc[];
-    uint64_t *bar = (uint64_t *)(smem_rtc + off_g + 2 * Gm::G_BYTES);
-    uint32_t *s_taddr = (uint32_t *)(smem_rtc + off_g + 2 * Gm::G_BYTES + 8);
-    int *s_abort = (int *)(smem_rtc + off_g + 2 * Gm::G_BYTES + 12);
+    uint64_t *bar = (uint64_t *)(smem_rtc + off_g + Gm::PARTS * Gm::G_BYTES);
+    uint32_t *s_taddr = (uint32_t *)(smem_rtc + off_g + Gm::PARTS * Gm::G_BYTES + 8);
+    int *s_abort = (int *)(smem_rtc + off_g + Gm::PARTS * Gm::G_BYTES + 12);
     const int tid = threadIdx.x;
     const uint4 *gsrc = gtab + Gm::GTAB_OFF / 16;
     uint4 *gdst = (uint4 *)(smem_rtc + off_g);
-    for (int i = tid; i < 2 * Gm::G_BYTES / 16; i += kRagThreads) gdst[i] = gsrc[i];
+    for (int i = tid; i < Gm::PARTS * Gm::G_BYTES / 16; i += kRagThreads) gdst[i] = gsrc[i];
     if (tid < 32) tmem_alloc(s_taddr, Lay::TMEM_COLS);
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -252,10 +252,7 @@ fft_ragged_tc_kernel(RagParams P, const uint4 *__restrict__ gtab, uint32_t off_g
     __syncthreads();
     tc_fence_after();
     TcState st;
-    st.a_hi = smem_rtc;
-    st.a_lo = smem_rtc + Lay::A_BYTES;
-    st.g_hi = smem_rtc + off_g;
-    st.g_lo = smem_rtc + off_g + Gm::G_BYTES;
+    tc_state_parts<KIND>(st, smem_rtc, Lay::A_BYTES, smem_rtc + off_g);
     st.bar = bar;
     st.abort = s_abort;
     st.err = P.error;  // a completion wait that gives up stops the whole launch
@@ -344,21 +341,25 @@ struct RaggedPlanImpl {
 };
 
 static int rag_tc_kind(const RaggedPlanImpl &p) { return tc_kind_of_precision(p.precision); }
+static size_t rag_tc_parts(int kind) { return kind == kTcBF16X6 ? 3 : 2; }
 static size_t rag_tc_a_bytes(int kind) {
     return (size_t)kRagThreads * (kind == kTcTF32 ? TcGeom<kTcTF32>::ROW_BYTES : TcGeom<kTcF16>::ROW_BYTES);
 }
 static size_t rag_tc_off_g(const RaggedPlanImpl &p) {
-    return (std::max(rag_smem_bytes(), 2 * rag_tc_a_bytes(rag_tc_kind(p))) + 1023) & ~(size_t)1023;
+    const int kind = rag_tc_kind(p);
+    return (std::max(rag_smem_bytes(), rag_tc_parts(kind) * rag_tc_a_bytes(kind)) + 1023) & ~(size_t)1023;
 }
 static size_t rag_tc_smem_bytes(const RaggedPlanImpl &p) {
-    const size_t g = rag_tc_kind(p) == kTcTF32 ? TcGeom<kTcTF32>::G_BYTES : TcGeom<kTcF16>::G_BYTES;
-    return rag_tc_off_g(p) + 2 * g + 64;
+    const int kind = rag_tc_kind(p);
+    const size_t g = kind == kTcTF32 ? TcGeom<kTcTF32>::G_BYTES : TcGeom<kTcF16>::G_BYTES;
+    return rag_tc_off_g(p) + rag_tc_parts(kind) * g + 64;
 }
 static const void *rag_kernel(const RaggedPlanImpl &p) {
     switch (p.precision) {
         case GBFFT_PREC_TC_FP16: return (const void *)fft_ragged_tc_kernel<kTcF16>;
         case GBFFT_PREC_TC_BF16X3: return (const void *)fft_ragged_tc_kernel<kTcBF16>;
         case GBFFT_PREC_TC_TF32: return (const void *)fft_ragged_tc_kernel<kTcTF32>;
+        case GBFFT_PREC_TC_BF16X6: return (const void *)fft_ragged_tc_kernel<kTcBF16X6>;
         default: return (const void *)fft_ragged_kernel;
     }
 }

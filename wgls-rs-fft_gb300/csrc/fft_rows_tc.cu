@@ -36,10 +36,11 @@ struct RowsTcCfg {
     static constexpr uint32_t TMEM_COLS = rtc_tmem_cols(NMMA);
     static constexpr size_t TILE_BYTES = (size_t)G * S::N * sizeof(float2);
     static constexpr size_t A_BYTES = (size_t)THREADS * Gm::ROW_BYTES;
-    // the hi/lo A operands alias the exchange tile (tc_dft16 waits for its readers)
-    static constexpr size_t REGION = ((2 * A_BYTES > TILE_BYTES ? 2 * A_BYTES : TILE_BYTES) + 1023) & ~(size_t)1023;
+    static constexpr size_t A_ALL = Gm::PARTS * A_BYTES;
+    // the A operand parts alias the exchange tile (tc_dft16 waits for its readers)
+    static constexpr size_t REGION = ((A_ALL > TILE_BYTES ? A_ALL : TILE_BYTES) + 1023) & ~(size_t)1023;
     static constexpr size_t OFF_G = REGION;
-    static constexpr size_t OFF_MISC = OFF_G + 2 * (size_t)Gm::G_BYTES;
+    static constexpr size_t OFF_MISC = OFF_G + Gm::PARTS * (size_t)Gm::G_BYTES;
     static constexpr size_t SMEM = OFF_MISC + 64;
     static constexpr int MINB = THREADS >= 1024 ? 1 : (THREADS >= 512 ? 2 : 4);
 };
@@ -58,7 +59,7 @@ fft_rows_tc_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *
     const int tid = threadIdx.x;
     const uint4 *gsrc = gtab + Gm::GTAB_OFF / 16;
     uint4 *gdst = (uint4 *)(smem_rtc + C::OFF_G);
-    for (int i = tid; i < 2 * Gm::G_BYTES / 16; i += C::THREADS) gdst[i] = gsrc[i];
+    for (int i = tid; i < Gm::PARTS * Gm::G_BYTES / 16; i += C::THREADS) gdst[i] = gsrc[i];
     if (tid < 32) tmem_alloc(s_taddr, C::TMEM_COLS);
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -68,10 +69,7 @@ fft_rows_tc_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *
     __syncthreads();
     tc_fence_after();
     TcState st;
-    st.a_hi = smem_rtc;
-    st.a_lo = smem_rtc + C::A_BYTES;
-    st.g_hi = smem_rtc + C::OFF_G;
-    st.g_lo = smem_rtc + C::OFF_G + Gm::G_BYTES;
+    tc_state_parts<KIND>(st, smem_rtc, C::A_BYTES, smem_rtc + C::OFF_G);
     st.bar = bar;
     st.abort = s_abort;
     st.err = err;
@@ -137,6 +135,7 @@ bool rows_tc_info_kind(int logn, RowsKernelInfo &k) {
 bool rows_tc_kernel_info(int logn, int precision, RowsKernelInfo &k) {
     switch (tc_kind_of_precision(precision)) {
         case kTcBF16: return rows_tc_info_kind<kTcBF16>(logn, k);
+        case kTcBF16X6: return rows_tc_info_kind<kTcBF16X6>(logn, k);
         case kTcTF32: return rows_tc_info_kind<kTcTF32>(logn, k);
         default: return rows_tc_info_kind<kTcF16>(logn, k);
     }

@@ -11,7 +11,7 @@
 //
 // Precision: A and G are split into hi + lo parts and
 // D = Ah.Gh + Ah.Gl + Al.Gh is accumulated in FP32 in tensor memory (the
-// Al.Gl term is below the FP32 rounding of the result).  Three operand kinds:
+// Al.Gl term is below the FP32 rounding of the result).  Four operand kinds:
 //   FP16 / BF16 (kind::f16): each row is first scaled by an exact power of two
 //     so that its largest component lies in [1, 2); FP16's range then always
 //     suffices and hi + lo carry 22 significant bits (BF16: 16 bits).
@@ -21,6 +21,11 @@
 //     is needed (three instructions per value; the 16-bit forms take a scale,
 //     and per pair of values two packed converts and two mixed-precision
 //     FMAs, plus the row maximum and the unscale).  About 22 significant bits.
+//   BF16 x 6 (kind::f16, BF16 operands): A and G split into three BF16 parts,
+//     hi + mid + lo (8 significant bits each, 24 together: FP32's
+//     significand), and D = Ah.Gh + Ah.Gm + Am.Gh + Ah.Gl + Al.Gh + Am.Gm, six
+//     products; the dropped terms Am.Gl, Al.Gm, Al.Gl are of order 2^-24
+//     relative.  BF16 has FP32's exponent range, so no scaling either.
 //
 // Operands live in shared memory in the canonical K-major, no-swizzle layout
 // of the tcgen05 matrix descriptors: core matrices of 8 rows x 16 bytes (8
@@ -39,7 +44,7 @@
 namespace gbfft {
 
 // Operand kinds of the split forms.
-enum : int { kTcF16 = 0, kTcBF16 = 1, kTcTF32 = 2 };
+enum : int { kTcF16 = 0, kTcBF16 = 1, kTcTF32 = 2, kTcBF16X6 = 3 };
 
 constexpr uint32_t kTcLbo = 128;  // bytes between K-adjacent core matrices
 
@@ -48,7 +53,9 @@ constexpr uint32_t kTcLbo = 128;  // bytes between K-adjacent core matrices
 // RADIX 32 (the 32-sample tiles) for the 16-bit kinds.
 template <int KIND, int RADIX = 16>
 struct TcGeom {
-    static_assert(RADIX == 16 || (RADIX == 32 && KIND != kTcTF32), "radix-32 operands are 16-bit");
+    static_assert(RADIX == 16 || (RADIX == 32 && (KIND == kTcF16 || KIND == kTcBF16)),
+                  "radix-32 operands: FP16 and BF16 hi+lo only");
+    static constexpr int PARTS = KIND == kTcBF16X6 ? 3 : 2;  // operand parts: hi, (mid,) lo
     static constexpr int VALS = 2 * RADIX;                 // values per row
     static constexpr int ELEM = KIND == kTcTF32 ? 4 : 2;  // bytes per value
     static constexpr int ROW_BYTES = VALS * ELEM;          // one A row
@@ -56,14 +63,15 @@ struct TcGeom {
     static constexpr uint32_t SBO = KB * 128u;             // bytes between row-adjacent core matrices
     static constexpr int G_BYTES = VALS * ROW_BYTES;       // one G part (hi or lo)
     static constexpr int NKSTEP = ROW_BYTES / 32;          // MMAs along K (32 bytes of K each)
-    // byte offset of the kind's [hi | lo] parts in the G table
+    // byte offset of the kind's [hi | lo (| mid)] parts in the G table
     static constexpr int GTAB_OFF = RADIX == 32 ? (KIND == kTcF16 ? 16384 : 32768)
-                                                : (KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 4096 : 8192));
+                                                : (KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 4096 :
+                                                                         (KIND == kTcTF32 ? 8192 : 49152)));
     // Instruction descriptor: D F32, A/B F16 (0) / BF16 (1) under kind::f16 or
     // TF32 (2) under kind::tf32, both K-major, M = 128, N = 2 RADIX.
-    static constexpr uint32_t IDESC = (1u << 4) | ((uint32_t)(KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 1 : 2)) << 7) |
-                                      ((uint32_t)(KIND == kTcF16 ? 0 : (KIND == kTcBF16 ? 1 : 2)) << 10) |
-                                      (((uint32_t)VALS >> 3) << 17) | ((128u >> 4) << 24);
+    static constexpr uint32_t ATYPE = KIND == kTcF16 ? 0u : (KIND == kTcTF32 ? 2u : 1u);
+    static constexpr uint32_t IDESC = (1u << 4) | (ATYPE << 7) | (ATYPE << 10) | (((uint32_t)VALS >> 3) << 17) |
+                                      ((128u >> 4) << 24);
     // Byte offset of value (row, k) of a K-major no-swizzle operand.
     __host__ __device__ static constexpr uint32_t elem_offset(uint32_t row, uint32_t k) {
         return ((row >> 3) * KB + ((k * ELEM) >> 4)) * 128u + (row & 7) * 16u + ((k * ELEM) & 15u);
@@ -176,6 +184,25 @@ __device__ __forceinline__ void tc_split2(float a, float b, uint32_t &hi, uint32
     }
 }
 
+// Three-part BF16 split of two values packed as pairs (a in the low half):
+// hi = RN(v), mid = RN(v - hi), lo = RN(v - hi - mid), each remainder exact in
+// FP32 (mixed-precision FMAs as in tc_split2), so hi + mid + lo keeps 24
+// significant bits of v.
+__device__ __forceinline__ void tc_split3_bf16(float a, float b, uint32_t &hi, uint32_t &mid, uint32_t &lo) {
+    float ra, rb, sa, sb;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(b), "f"(a));
+    asm("{\n\t.reg .b16 h0, h1, m;\n\tmov.b32 {h0, h1}, %2;\n\tmov.b16 m, 0xBF80;\n\t"
+        "fma.rn.f32.bf16 %0, h0, m, %3;\n\tfma.rn.f32.bf16 %1, h1, m, %4;\n\t}"
+        : "=f"(ra), "=f"(rb)
+        : "r"(hi), "f"(a), "f"(b));
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(mid) : "f"(rb), "f"(ra));
+    asm("{\n\t.reg .b16 h0, h1, m;\n\tmov.b32 {h0, h1}, %2;\n\tmov.b16 m, 0xBF80;\n\t"
+        "fma.rn.f32.bf16 %0, h0, m, %3;\n\tfma.rn.f32.bf16 %1, h1, m, %4;\n\t}"
+        : "=f"(sa), "=f"(sb)
+        : "r"(mid), "f"(ra), "f"(rb));
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(sb), "f"(sa));
+}
+
 // TF32 split: hi = x rounded to the nearest TF32 value (sign, exponent and 10
 // explicit mantissa bits; ties away from zero), lo = x - hi, exact in FP32 and
 // of either sign, |lo| <= 2^-11 |x|.  Rounding (rather than clearing the low
@@ -191,8 +218,10 @@ __device__ __forceinline__ void tc_split_tf32(float x, uint32_t &hi, uint32_t &l
 struct TcState {
     uint8_t *a_hi;       // [threads rows][32 values], canonical layout
     uint8_t *a_lo;
+    uint8_t *a_mid;      // BF16 x 6 only
     const uint8_t *g_hi; // [32][32]
     const uint8_t *g_lo;
+    const uint8_t *g_mid;
     uint64_t *bar;       // MMA completion barrier
     int *abort;          // shared flag: a completion wait gave up
     uint32_t *err;       // global error flag (set on timeout)
@@ -212,7 +241,27 @@ __device__ __forceinline__ void tc_dft(float2 (&x)[RADIX], TcState &s) {
     constexpr int V = Gm::VALS;
     const uint32_t r = threadIdx.x;
     float up = 1.f;
-    if constexpr (KIND == kTcTF32) {
+    if constexpr (KIND == kTcBF16X6) {
+        // no scaling (BF16 has FP32's exponent range); three parts per value.
+        // A shares its bytes with the FP32 exchange tile: every thread must
+        // have finished reading its exchange inputs before any thread writes A.
+        __syncthreads();
+#pragma unroll
+        for (int kb = 0; kb < V / 8; ++kb) {
+            uint32_t hi[4], mi[4], lo[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int k = 8 * kb + 2 * i;
+                const float2 a = x[k % RADIX], b = x[(k + 1) % RADIX];
+                if (k < RADIX) tc_split3_bf16(a.x, b.x, hi[i], mi[i], lo[i]);
+                else tc_split3_bf16(a.y, b.y, hi[i], mi[i], lo[i]);
+            }
+            const uint32_t off = Gm::elem_offset(r, 8 * kb);
+            *(uint4 *)(s.a_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+            *(uint4 *)(s.a_mid + off) = make_uint4(mi[0], mi[1], mi[2], mi[3]);
+            *(uint4 *)(s.a_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        }
+    } else if constexpr (KIND == kTcTF32) {
         // A shares its bytes with the FP32 exchange tile: every thread must
         // have finished reading its exchange inputs before any thread writes A.
         __syncthreads();
@@ -276,15 +325,31 @@ __device__ __forceinline__ void tc_dft(float2 (&x)[RADIX], TcState &s) {
                 const uint32_t d = s.taddr + mb * V;
                 const uint32_t arow = mb * 128 * Gm::ROW_BYTES;  // 128 rows = 16 row blocks
                 uint32_t acc = 0;
+                if constexpr (KIND == kTcBF16X6) {
+                    // hh, hm, mh, hl, lh, mm
+                    const uint32_t am = smem_u32(s.a_mid), gm = smem_u32(s.g_mid);
+                    const uint32_t pa[6] = {ah, ah, am, ah, al, am};
+                    const uint32_t pg[6] = {gh, gm, gh, gl, gh, gm};
 #pragma unroll
-                for (int part = 0; part < 3; ++part) {
-                    const uint32_t a = (part == 2 ? al : ah) + arow;
-                    const uint32_t g = part == 1 ? gl : gh;
+                    for (int part = 0; part < 6; ++part) {
 #pragma unroll
-                    for (uint32_t ks = 0; ks < (uint32_t)Gm::NKSTEP; ++ks) {  // 32 bytes of K per MMA
-                        tc_mma<KIND>(d, tc_smem_desc(a + ks * 2 * kTcLbo, Gm::SBO),
-                                     tc_smem_desc(g + ks * 2 * kTcLbo, Gm::SBO), Gm::IDESC, acc);
-                        acc = 1;
+                        for (uint32_t ks = 0; ks < (uint32_t)Gm::NKSTEP; ++ks) {
+                            tc_mma<KIND>(d, tc_smem_desc(pa[part] + arow + ks * 2 * kTcLbo, Gm::SBO),
+                                         tc_smem_desc(pg[part] + ks * 2 * kTcLbo, Gm::SBO), Gm::IDESC, acc);
+                            acc = 1;
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int part = 0; part < 3; ++part) {
+                        const uint32_t a = (part == 2 ? al : ah) + arow;
+                        const uint32_t g = part == 1 ? gl : gh;
+#pragma unroll
+                        for (uint32_t ks = 0; ks < (uint32_t)Gm::NKSTEP; ++ks) {  // 32 bytes of K per MMA
+                            tc_mma<KIND>(d, tc_smem_desc(a + ks * 2 * kTcLbo, Gm::SBO),
+                                         tc_smem_desc(g + ks * 2 * kTcLbo, Gm::SBO), Gm::IDESC, acc);
+                            acc = 1;
+                        }
                     }
                 }
             }
@@ -351,7 +416,21 @@ struct DftTc32 {
 
 // gbfft_precision value -> operand kind
 __host__ __device__ constexpr int tc_kind_of_precision(int precision) {
-    return precision == 2 ? kTcBF16 : (precision == 3 ? kTcTF32 : kTcF16);
+    return precision == 2 ? kTcBF16 : (precision == 3 ? kTcTF32 : (precision == 4 ? kTcBF16X6 : kTcF16));
+}
+
+// Operand pointers of a TcState laid out as PARTS A parts of a_bytes each from
+// `a`, and PARTS G parts from `g` (order hi, lo, then mid), for the geometry of
+// RADIX-point DFTs.
+template <int KIND, int RADIX = 16>
+__device__ __forceinline__ void tc_state_parts(TcState &st, uint8_t *a, size_t a_bytes, const uint8_t *g) {
+    using Gm = TcGeom<KIND, RADIX>;
+    st.a_hi = a;
+    st.a_lo = a + a_bytes;
+    st.a_mid = Gm::PARTS == 3 ? a + 2 * a_bytes : nullptr;
+    st.g_hi = g;
+    st.g_lo = g + Gm::G_BYTES;
+    st.g_mid = Gm::PARTS == 3 ? g + 2 * Gm::G_BYTES : nullptr;
 }
 
 constexpr uint32_t kTcSpinLimit = 1u << 20;  // polls of an MMA completion that takes microseconds

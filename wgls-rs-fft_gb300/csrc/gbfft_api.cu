@@ -649,6 +649,7 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
         if (!strcmp(c, "tc_fp16")) ctx->precision = GBFFT_PREC_TC_FP16;
         else if (!strcmp(c, "tc_bf16x3")) ctx->precision = GBFFT_PREC_TC_BF16X3;
         else if (!strcmp(c, "tc_tf32")) ctx->precision = GBFFT_PREC_TC_TF32;
+        else if (!strcmp(c, "tc_bf16x6")) ctx->precision = GBFFT_PREC_TC_BF16X6;
     }
     if (const char *c = getenv("GBFFT_HOST_CHUNK_BYTES")) {
         const long long v = atoll(c);
@@ -729,7 +730,7 @@ int gbfft_set_noise(gbfft_ctx *ctx, uint32_t seed, float sigma) {
 int gbfft_set_precision(gbfft_ctx *ctx, int precision) {
     if (!ctx) return GBFFT_ERR_INVALID_ARGUMENT;
     if (precision != GBFFT_PREC_FP32 && precision != GBFFT_PREC_TC_FP16 && precision != GBFFT_PREC_TC_BF16X3 &&
-        precision != GBFFT_PREC_TC_TF32)
+        precision != GBFFT_PREC_TC_TF32 && precision != GBFFT_PREC_TC_BF16X6)
         return fail(ctx, GBFFT_ERR_INVALID_ARGUMENT, "precision %d is not a gbfft_precision", precision);
     ctx->precision = precision;
     return GBFFT_OK;

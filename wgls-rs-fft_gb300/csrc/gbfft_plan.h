@@ -133,7 +133,7 @@ cudaError_t rows_tc_launch(const RowsKernelInfo &k, const float2 *in, float2 *ou
                            cudaStream_t stream, LoadOps ops);
 // G table: radix 16: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (2 KB each), [TF32 hi | TF32 lo]
 // (4 KB each); radix 32: [FP16 hi | FP16 lo | BF16 hi | BF16 lo] (8 KB each)
-constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096 + 4 * 8192;
+constexpr size_t kTcGtabBytes = 4 * 2048 + 2 * 4096 + 4 * 8192 + 3 * 2048;  // ... + BF16 x 6 parts
 
 // fft_fused2.cu, fft_fused3.cu
 // loge 5: tiles of 32 samples a thread (radix-32 sub-passes), pairs with a radix-2^9/2^10 pass

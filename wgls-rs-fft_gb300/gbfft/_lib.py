@@ -19,6 +19,7 @@ PREC_FP32 = 0
 PREC_TC_FP16 = 1
 PREC_TC_BF16X3 = 2
 PREC_TC_TF32 = 3
+PREC_TC_BF16X6 = 4
 WINDOW_NONE = 0
 WINDOW_HANN = 1
 

@@ -21,6 +21,7 @@ pub const GBFFT_PREC_FP32: c_int = 0;
 pub const GBFFT_PREC_TC_FP16: c_int = 1;
 pub const GBFFT_PREC_TC_BF16X3: c_int = 2;
 pub const GBFFT_PREC_TC_TF32: c_int = 3;
+pub const GBFFT_PREC_TC_BF16X6: c_int = 4;
 
 pub const GBFFT_RAGGED_OPT_SPIN_LIMIT: c_int = 1;
 pub const GBFFT_RAGGED_OPT_TEST_DROP_PRODUCERS: c_int = 2;

@@ -32,6 +32,8 @@ pub enum Precision {
     TcBf16x3,
     /// The same with TF32 hi+lo operands.
     TcTf32,
+    /// BF16 operands split in three (hi + mid + lo), six products.
+    TcBf16x6,
 }
 
 impl Precision {
@@ -41,6 +43,7 @@ impl Precision {
             Precision::TcFp16 => GBFFT_PREC_TC_FP16,
             Precision::TcBf16x3 => GBFFT_PREC_TC_BF16X3,
             Precision::TcTf32 => GBFFT_PREC_TC_TF32,
+            Precision::TcBf16x6 => GBFFT_PREC_TC_BF16X6,
         }
     }
 }

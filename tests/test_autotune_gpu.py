@@ -206,6 +206,38 @@ def test_three_pass_first_pass_8_columns(tmp_path, monkeypatch, oracle, lib_buil
         assert oracle.rel_l2(outs[3][0], ref) <= TOL_REL_L2
 
 
+@pytest.mark.parametrize("logn,batch", [(25, 2), (26, 1)])
+def test_three_pass_first_pass_tma(tmp_path, monkeypatch, oracle, lib_built, logn, batch):
+    """The 8-column, 32-samples-a-thread first pass of N = 2^25 / 2^26 with its
+    input tile brought into shared memory by the tensor memory accelerator
+    (tiled copies of a [256 rows][8 columns] box of a 3-D tensor map; plan
+    key "tma": 1, the default) against the same pass with 8-byte loads
+    ("tma": 0): the same bits in both directions, and the FP64 gate."""
+    import numpy as np
+
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=1350 + logn)
+    outs = {}
+    for tma in (0, 1):
+        cache = tmp_path / f"tune_tma{tma}.jsonl"
+        lines = []
+        for d in (gbfft.FORWARD, gbfft.INVERSE):
+            line = json.loads(_cache_line(logn, batch, d, 10, 0, tile=3, loge=5))
+            line["fused"] = 1
+            line["tma"] = tma
+            line["seconds"] = line.pop("seconds")  # key order as the library writes it
+            lines.append(json.dumps(line))
+        cache.write_text("\n".join(lines) + "\n")
+        monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+        with gbfft.Context(0) as ctx:
+            outs[tma] = [ctx.c2c_host(x, d) for d in (gbfft.FORWARD, gbfft.INVERSE)]
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    for y, inv in zip(outs[1], (False, True)):
+        assert oracle.rel_l2(y, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2
+
+
 def test_three_pass_first_pass_unaligned_input(oracle, lib_built):
     """The device entry takes any 8-byte aligned input.  For N = 2^25 (three
     passes, the 8-column first pass, whose 16-byte stores go to the plan's

@@ -22,10 +22,14 @@
 // The first factor is one lookup per thread; the second depends only on the
 // column and e, so the CTA builds it once into a padded 16 x 17 shared table.
 // Both come from two FP64-built tables (W_N^i for i < 2^s and W_N^{i 2^s}).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"
+#include "fft_tc.cuh"
 #include "fft_tiles.cuh"
 
 namespace gbfft {
@@ -110,9 +114,117 @@ fft_pass_persistent_kernel(const float2 *in, float2 *out, int logn, int logp, co
     }
 }
 
+// First pass of radix 2^9 / 2^10 (N = 2^25, 2^26) whose input tile -- 8
+// adjacent columns x R rows, R row segments of 64 bytes 2^(logn - LOGR) * 8
+// bytes apart -- is brought into shared memory by the tensor memory
+// accelerator: R / 256 tiled copies of a [256 rows][8 columns] box of a 3-D
+// tensor map over the input (float32 elements: 2 N / R x R x batch), issued
+// by one thread and completing on one mbarrier.  The LDG form issues R * 8 / 8
+// loads of 8 bytes a CTA (32 a thread) and is held back by the global-load
+// queue; here the SM issues four instructions a tile and the copy engine of
+// the TMA generates the strided addresses.  The wait is bounded: on expiry
+// the launch raises the error flag (GBFFT_ERR_TIMEOUT on the host), waits
+// once more, bounded, for its copies and skips the tile.
+constexpr int kTmaBoxRows = 256;
+constexpr uint32_t kTmaSpinLimit = 1u << 20;
+
+template <int LOGR, int LE>
+struct PassTmaCfg {
+    using C = PassCfg<LOGR, LE, 3>;
+    static constexpr size_t OFF_BAR = (C::SMEM + 15) & ~(size_t)15;
+    static constexpr size_t SMEM = OFF_BAR + 16;
+    static constexpr uint32_t TILE_BYTES = (1u << LOGR) * 8u * (uint32_t)sizeof(float2);
+};
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+template <int LOGR, int LE>
+__global__ void __launch_bounds__(PassCfg<LOGR, LE, 3>::THREADS, PassCfg<LOGR, LE, 3>::MINB)
+fft_pass_first_tma_kernel(const __grid_constant__ CUtensorMap map, float2 *out, int logn,
+                          const float2 *__restrict__ tw, const float2 *__restrict__ tw_lo,
+                          const float2 *__restrict__ tw_hi, int tw_split, float in_im_sign, LoadOps ops,
+                          uint32_t *err) {
+    using T = PassTmaCfg<LOGR, LE>;
+    constexpr int R = 1 << LOGR;
+    extern __shared__ __align__(1024) float2 smem_pass[];
+    uint64_t *bar = (uint64_t *)((char *)smem_pass + T::OFF_BAR);
+    int *s_fail = (int *)((char *)smem_pass + T::OFF_BAR + 8);
+    const int lognc = logn - LOGR;
+    const uint64_t tile = blockIdx.x;
+    const uint64_t b = tile >> (lognc - 3);
+    const uint32_t col0 = (uint32_t)(tile & ((1ull << (lognc - 3)) - 1)) << 3;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *s_fail = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                     "r"(T::TILE_BYTES)
+                     : "memory");
+#pragma unroll
+        for (int k = 0; k < R / kTmaBoxRows; ++k)
+            tma_load_3d(smem_u32(smem_pass + k * kTmaBoxRows * 8), &map, (int)(2 * col0), k * kTmaBoxRows, (int)b,
+                        smem_u32(bar));
+    }
+    uint32_t polls = 0;
+    bool done = mbar_try_wait(bar, 0);
+    while (!done && ++polls < kTmaSpinLimit) done = mbar_try_wait(bar, 0);
+    if (!done) *s_fail = 1;
+    __syncthreads();
+    if (*s_fail) {
+        if (threadIdx.x == 0) {
+            atomicExch(err, 4u);
+            for (uint32_t n = 0; n < kTmaSpinLimit && !mbar_try_wait(bar, 0); ++n) {
+            }
+        }
+        __syncthreads();
+        return;
+    }
+    PassArgs a;
+    a.src = nullptr;
+    a.dst = out + (b << logn);
+    a.logn = logn;
+    a.logp = 0;
+    a.col0 = col0;
+    a.tw_sub = tw;
+    a.tw_lo = tw_lo;
+    a.tw_hi = tw_hi;
+    a.tw_split = tw_split;
+    a.in_im = in_im_sign;
+    a.out_re = 1.0f;
+    a.out_im = 1.0f;
+    a.coherent_load = false;
+    a.row = (uint32_t)b;
+    a.ops = ops;
+    pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_pass);
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+        }
+        return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }();
+    return fn;
+}
 
 template <int LOGR, int LE = 4>
 static void pass_describe(PassDesc &d, bool first) {
@@ -127,9 +239,11 @@ static void pass_describe(PassDesc &d, bool first) {
     d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
 }
 
-// First pass of 8 columns a CTA.
+// First pass of 8 columns a CTA; tma: its input tile comes by the tensor
+// memory accelerator (32 samples a thread only), the LDG kernel kept as the
+// form for inputs that are not 16-byte aligned.
 template <int LOGR, int LE>
-static void pass_describe_first8(PassDesc &d) {
+static void pass_describe_first8(PassDesc &d, bool tma) {
     using C = PassCfg<LOGR, LE, 3>;
     d.fn = (const void *)fft_pass_kernel<LOGR, true, LE, 3>;
     d.fn_persistent = (const void *)fft_pass_persistent_kernel<LOGR, true, LE, 3>;
@@ -138,17 +252,24 @@ static void pass_describe_first8(PassDesc &d) {
     d.cols = C::COLS;
     d.nseg = subcfg_segments<LOGR, LE>(d.segs, 0);
     d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
+    if constexpr (LE == 5) {
+        if (tma) {
+            d.fn_tma = (const void *)fft_pass_first_tma_kernel<LOGR, LE>;
+            d.smem_tma = PassTmaCfg<LOGR, LE>::SMEM;
+        }
+    }
 }
 
-bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge, int cols_log) {
+bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge, int cols_log, bool tma) {
     d.logr = logr;
+    if (tma && !(first && cols_log == 3 && loge == 5)) return false;
     if (cols_log == 3) {  // first passes of radix 2^9 / 2^10 only
         if (!first) return false;
         switch (logr * 10 + loge) {
-            case 94: pass_describe_first8<9, 4>(d); return true;
-            case 95: pass_describe_first8<9, 5>(d); return true;
-            case 104: pass_describe_first8<10, 4>(d); return true;
-            case 105: pass_describe_first8<10, 5>(d); return true;
+            case 94: pass_describe_first8<9, 4>(d, tma); return true;
+            case 95: pass_describe_first8<9, 5>(d, tma); return true;
+            case 104: pass_describe_first8<10, 4>(d, tma); return true;
+            case 105: pass_describe_first8<10, 5>(d, tma); return true;
             default: return false;
         }
     }
@@ -174,6 +295,10 @@ bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge, int cols_log)
 
 cudaError_t pass_prepare(PassDesc &d) {
     cudaError_t e = cudaSuccess;
+    if (d.fn_tma && d.smem_tma > 48 * 1024) {
+        e = cudaFuncSetAttribute(d.fn_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem_tma);
+        if (e != cudaSuccess) return e;
+    }
     if (d.smem > 48 * 1024) {
         e = cudaFuncSetAttribute(d.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem);
         if (e == cudaSuccess && d.fn_persistent)
@@ -187,12 +312,32 @@ cudaError_t pass_prepare(PassDesc &d) {
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                         float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
-                        bool persistent, int sms, LoadOps ops) {
+                        bool persistent, int sms, LoadOps ops, uint32_t *err) {
     uint64_t tiles = (batch << (logn - d.logr)) / (uint64_t)d.cols;
     if (tiles == 0) return cudaSuccess;
     // the 8-column first pass stores 16-byte pairs
     if (d.cols < kCols && ((uintptr_t)out & 15u)) return cudaErrorMisalignedAddress;
     int logp = d.logp;
+    // tensor-map first pass: needs a 16-byte aligned input (the map's base
+    // address), an error flag for its bounded wait, and the driver's encoder;
+    // otherwise the LDG kernel runs
+    PFN_cuTensorMapEncodeTiled_v12000 encode = d.fn_tma ? tensor_map_encoder() : nullptr;
+    if (d.fn_tma && encode && err && ((uintptr_t)in & 15u) == 0 && tiles <= 0x7fffffffull && batch <= 0xffffffffull) {
+        const int lognc = logn - d.logr;
+        // dims (innermost first): 2 N / R floats (the row), R rows, batch
+        const cuuint64_t dims[3] = {2ull << lognc, 1ull << d.logr, batch};
+        const cuuint64_t strides[2] = {(2ull << lognc) * sizeof(float), (1ull << logn) * sizeof(float2)};
+        const cuuint32_t box[3] = {16, (cuuint32_t)std::min(1 << d.logr, kTmaBoxRows), 1};
+        const cuuint32_t estr[3] = {1, 1, 1};
+        alignas(64) CUtensorMap map;
+        if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)in, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+            void *args[] = {(void *)&map,  (void *)&out,   (void *)&logn,     (void *)&tw_sub,     (void *)&tw_lo,
+                            (void *)&tw_hi, (void *)&tw_split, (void *)&in_im_sign, (void *)&ops, (void *)&err};
+            return cudaLaunchKernel(d.fn_tma, dim3((unsigned)tiles), dim3(d.threads), args, d.smem_tma, stream);
+        }
+    }
     if (persistent && d.fn_persistent && d.persist_ctas_per_sm > 0 && sms > 0) {
         const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)d.persist_ctas_per_sm * (uint64_t)sms);
         void *args[] = {(void *)&in,    (void *)&out,   (void *)&logn,     (void *)&logp,

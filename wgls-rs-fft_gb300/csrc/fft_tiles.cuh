@@ -208,8 +208,11 @@ struct PassArgs {
 // samples a thread holds (SubCfg; the sub-pass tables in a.tw_sub follow it).
 // CL: log2 of the columns a group takes; 8 columns still move 64 contiguous
 // bytes per row and halve the tile, so a radix-2^9/2^10 tile fits twice per SM.
+// PRE: the input tile is already in shared memory as [row][2^CL columns] at
+// the group's exchange buffer (NG = 1; brought in by the tensor memory
+// accelerator), so the samples are read from there instead of from a.src.
 template <int LOGR, int NG, bool FIRST, class Eng = DftRegs, int LOGN_CT = 0, int LOGP_CT = -1, int LE = 4,
-          int CL = kColsLog>
+          int CL = kColsLog, bool PRE = false>
 __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng eng = Eng()) {
     using C = SubCfg<LOGR, LE>;
     using K = PassTileCfg<LOGR, NG, LE, CL>;
@@ -231,7 +234,12 @@ __device__ __forceinline__ void pass_tile(const PassArgs &a, float2 *smem, Eng e
 
     float2 v[E];
     // All E loads first, back to back; options are applied afterwards.
-    if (a.coherent_load) {
+    if constexpr (PRE) {
+        static_assert(NG == 1, "one column group per CTA");
+#pragma unroll
+        for (int e = 0; e < E; ++e) v[e] = buf[((t + T * e) << CL) + c];
+        __syncthreads();  // the tile is the exchange buffer: every thread has its samples first
+    } else if (a.coherent_load) {
 #pragma unroll
         for (int e = 0; e < E; ++e) v[e] = __ldcg(a.src + j + ((uint64_t)(t + T * e) << lognc));
     } else {

@@ -351,9 +351,9 @@ int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *
         if (ctx->tune_verbose)
             fprintf(stderr,
                     "gbfft autotune N=2^%d batch=%llu dir=%d prec=%d max_logr=%d persistent=%d fused=%d "
-                    "tile=%d loge=%d: %.3f us\n",
+                    "tile=%d loge=%d tma=%d: %.3f us\n",
                     logn, (unsigned long long)batch, direction, ctx->precision, v.max_logr, v.persistent ? 1 : 0,
-                    v.fused ? 1 : 0, v.tile, v.loge,
+                    v.fused ? 1 : 0, v.tile, v.loge, v.tma ? 1 : 0,
                     s * 1e6);
         if (s < best) {
             best = s;
@@ -370,9 +370,9 @@ int autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, double *
             fprintf(f,
                     "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
                     "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"tile\": %d, \"loge\": %d, "
-                    "\"seconds\": %.9g}\n",
+                    "\"tma\": %d, \"seconds\": %.9g}\n",
                     logn, ctx->precision, direction, log2floor(batch), best_v.max_logr, best_v.persistent ? 1 : 0,
-                    best_v.fused ? 1 : 0, best_v.tile, best_v.loge,
+                    best_v.fused ? 1 : 0, best_v.tile, best_v.loge, best_v.tma ? 1 : 0,
                     best);
             fclose(f);
         }
@@ -385,20 +385,24 @@ void load_tune_cache(gbfft_ctx *ctx) {
     if (!f) return;
     char line[512];
     while (fgets(line, sizeof line, f)) {
-        int logn, prec, dir, blog, mlr, pers, fused, tile, loge = 4;
+        int logn, prec, dir, blog, mlr, pers, fused, tile, loge = 4, tma = 0;
         double sec;
-        // lines written before the "loge" key existed read as loge 4
+        // lines written before the "loge" / "tma" keys existed read as loge 4 / tma 0
         const char *head =
             "{\"arch\": \"sm_103\", \"logn\": %d, \"precision\": %d, \"direction\": %d, \"batch_log2\": %d, "
             "\"max_logr\": %d, \"persistent\": %d, \"fused\": %d, \"tile\": %d, ";
+        const std::string with_tma = std::string(head) + "\"loge\": %d, \"tma\": %d, \"seconds\": %lf}";
         const std::string with_loge = std::string(head) + "\"loge\": %d, \"seconds\": %lf}";
         const std::string without = std::string(head) + "\"seconds\": %lf}";
-        const bool ok = sscanf(line, with_loge.c_str(), &logn, &prec, &dir, &blog, &mlr, &pers, &fused, &tile, &loge,
-                               &sec) == 10 ||
+        const bool ok = sscanf(line, with_tma.c_str(), &logn, &prec, &dir, &blog, &mlr, &pers, &fused, &tile, &loge,
+                               &tma, &sec) == 11 ||
+                        (tma = 0, sscanf(line, with_loge.c_str(), &logn, &prec, &dir, &blog, &mlr, &pers, &fused,
+                                         &tile, &loge, &sec) == 10) ||
                         (loge = 4, sscanf(line, without.c_str(), &logn, &prec, &dir, &blog, &mlr, &pers, &fused, &tile,
                                           &sec) == 9);
         if (ok)
-            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] = PlanVariant{mlr, pers != 0, fused != 0, tile, loge};
+            ctx->tuned[std::make_tuple(logn, prec, dir, blog)] =
+                PlanVariant{mlr, pers != 0, fused != 0, tile, loge, tma != 0};
     }
     fclose(f);
 }

@@ -114,6 +114,9 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         // 2^26: 118.5 vs 115.9, 2^25: 131.0 vs 128.7 GSa/s
         PassDesc pd;
         const bool e32 = pass_kernel_info(logn - 16, true, pd, 5);
+        // its 8-column input tile brought in by the TMA (four tiled copies a
+        // tile instead of 32 8-byte loads a thread)
+        if (pass_kernel_info(logn - 16, true, pd, 5, 3, true)) c.push_back(PlanVariant{10, false, true, 3, 5, true});
         if (pass_kernel_info(logn - 16, true, pd, 5, 3)) c.push_back(PlanVariant{10, false, true, 3, 5});
         if (e32) c.push_back(PlanVariant{10, false, true, 0, 5});
         c.push_back(PlanVariant{10, false, true});
@@ -204,7 +207,7 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
             PassDesc d;
             const bool ok = tc ? pass_tc_kernel_info(parts[i], i == 0, precision, d)
                                : pass_kernel_info(parts[i], i == 0, d, (fused3 && i == 0) ? v.loge : 4,
-                                                  (fused3 && i == 0 && v.tile) ? v.tile : 4);
+                                                  (fused3 && i == 0 && v.tile) ? v.tile : 4, fused3 && i == 0 && v.tma);
             if (!ok) {
                 why = std::string("no ") + (tc ? "tensor-core " : "") + "pass kernel for radix 2^" +
                       std::to_string(parts[i]);
@@ -308,7 +311,7 @@ int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, i
             const PassDesc &d0 = p.passes[0];
             e = pass_launch(d0, in, (float2 *)ws.ptr, batch, p.logn, p.tw + d0.sub_tw_offset, p.tw + p.tw_lo_offset,
                             p.tw + p.tw_hi_offset, p.tw_split, inv ? -1.0f : 1.0f, 1.0f, 1.0f, stream,
-                            p.variant.persistent, p.sms, ops);
+                            p.variant.persistent, p.sms, ops, err);
             if (e != cudaSuccess) {
                 why = cudaGetErrorString(e);
                 return GBFFT_ERR_CUDA;

@@ -34,6 +34,8 @@ struct PassDesc {
     int nseg = 0;
     int tw_entries = 0;
     bool tc = false;                    // radix-16 butterflies on the tensor cores
+    const void *fn_tma = nullptr;       // first pass with its input tile brought in by the TMA
+    size_t smem_tma = 0;
 };
 
 // Two consecutive passes in one persistent launch whose queue alternates the
@@ -71,16 +73,18 @@ struct PlanVariant {
     int tile = 0;  // single pass: log2 of the samples a CTA moves (0: 2^12), i.e. transforms per CTA;
                    // three passes: log2 of the columns a first-pass CTA takes (0: 16)
     int loge = 4;  // single pass: log2 of the samples a thread holds (5: radix-32 sub-passes, N = 2^13, 2^14)
+    bool tma = false;  // three passes, 8-column first pass: input tile brought in by the TMA
     bool operator<(const PlanVariant &o) const {
         if (max_logr != o.max_logr) return max_logr < o.max_logr;
         if (persistent != o.persistent) return persistent < o.persistent;
         if (fused != o.fused) return fused < o.fused;
         if (tile != o.tile) return tile < o.tile;
-        return loge < o.loge;
+        if (loge != o.loge) return loge < o.loge;
+        return tma < o.tma;
     }
     bool operator==(const PlanVariant &o) const {
         return max_logr == o.max_logr && persistent == o.persistent && fused == o.fused && tile == o.tile &&
-               loge == o.loge;
+               loge == o.loge && tma == o.tma;
     }
 };
 
@@ -107,12 +111,13 @@ struct Plan {
 
 // fft_passes.cu
 // loge 5: 32 samples a thread, for the first pass of radix 2^9 / 2^10 only
-bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge = 4, int cols_log = 4);
+bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge = 4, int cols_log = 4, bool tma = false);
 cudaError_t pass_prepare(PassDesc &d);
 cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64_t batch, int logn,
                         const float2 *tw_sub, const float2 *tw_lo, const float2 *tw_hi, int tw_split,
                         float in_im_sign, float out_re_scale, float out_im_scale, cudaStream_t stream,
-                        bool persistent = false, int sms = 0, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
+                        bool persistent = false, int sms = 0, LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u},
+                        uint32_t *err = nullptr);
 
 // fft_passes_tc.cu (split-precision tensor-core form)
 bool pass_tc_kernel_info(int logr, bool first, int precision, PassDesc &d);

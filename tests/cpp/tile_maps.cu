@@ -156,7 +156,7 @@ void check_rows_exchanges(bool &ok, int &worst) {
                     std::vector<int> a;
                     for (int l = 0; l < 32; ++l) {
                         const int tid = 32 * w + l, g = tid / T, t = tid % T;
-                        a.push_back(g * N + swz<C::LOGE>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP));
+                        a.push_back(g * rows_buf_stride<LOGN, LE>() + swz<C::LOGE>(subpass_out_pos<PR, PP, C::LOGT>(t, b, q), PP));
                     }
                     worst = std::max(worst, wavefronts(a));
                 }
@@ -164,7 +164,7 @@ void check_rows_exchanges(bool &ok, int &worst) {
                 std::vector<int> a;
                 for (int l = 0; l < 32; ++l) {
                     const int tid = 32 * w + l, g = tid / T, t = tid % T;
-                    a.push_back(g * N + swz<C::LOGE>(t + T * e, PP));
+                    a.push_back(g * rows_buf_stride<LOGN, LE>() + swz<C::LOGE>(t + T * e, PP));
                 }
                 worst = std::max(worst, wavefronts(a));
             }

@@ -8,10 +8,10 @@ index functions (no GPU needed).
 Checked: every exchange and the first-pass output staging are bijections onto
 the tile, read back where they were written (the staging as adjacent 16-byte
 pairs for 8 columns), and each warp access takes the fewest shared-memory
-wavefronts its width allows (2 for 8-byte lanes, 4 for 16-byte lanes).  The
-one known exception is pinned: single-pass N = 2^5 / 2^6 / 2^7, where a warp
-spans 16 / 8 / 4 transforms whose buffers start on the same banks (16, 8 and
-4 wavefronts)."""
+wavefronts its width allows (2 for 8-byte lanes, 4 for 16-byte lanes),
+including single-pass N = 2^5 / 2^6 / 2^7, where a warp spans 16 / 8 / 4
+transforms and each transform's buffer is padded by one sample a thread so
+that the buffers start on different banks."""
 import os
 import shutil
 import subprocess
@@ -36,7 +36,7 @@ def test_pass_tile_index_maps(tmp_path):
     single = [tuple(int(v) for v in line.split()[1:]) for line in out if line.startswith("rows ")]
     passes = [tuple(int(v) for v in line.split()[1:]) for line in out if line.startswith("pass ")]
     assert len(single) == 13 and len(passes) == 14
-    small = {4: 0, 5: 16, 6: 8, 7: 4}  # no exchange at 2^4; warps spanning several transforms below 2^8
+    small = {4: 0}  # no exchange at 2^4
     for logn, le, ok, w in single:
         assert ok == 1, (logn, le)
         assert w == small.get(logn, 2), ("single-pass exchange wavefronts", logn, le, w)

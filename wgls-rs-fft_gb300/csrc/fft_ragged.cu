@@ -280,7 +280,7 @@ fft_ragged_tc_kernel(RagParams P, const uint4 *__restrict__ gtab, uint32_t off_g
 // ---------------------------------------------------------------------------
 
 static size_t rag_smem_bytes() {
-    size_t m = (size_t)kRagThreads * 16 * sizeof(float2);  // rows items
+    size_t m = (size_t)kRagThreads * 17 * sizeof(float2);  // rows items (padded buffers: at most 17 a thread)
     for (int lr = 7; lr <= 9; ++lr) {
         const int ng = rag_groups(lr);
         m = std::max(m, ((size_t)ng * kCols * (1u << lr) + (size_t)ng * kCols * 17) * sizeof(float2));

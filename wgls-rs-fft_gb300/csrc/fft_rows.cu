@@ -38,7 +38,7 @@ struct RowsCfg : SubCfg<LOGN, LE> {
     static constexpr int THREADS = G * S::T;
     static constexpr int REGS = LE == 4 ? 64 : 128;  // registers a thread
     static constexpr int MINB = THREADS * REGS >= 65536 ? 1 : 65536 / (THREADS * REGS);
-    static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * S::N * sizeof(float2) : 0;
+    static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * rows_buf_stride<LOGN, LE>() * sizeof(float2) : 0;
 };
 
 // DIRC: -1 forward, +1 inverse (a launch has one direction, so the sign and

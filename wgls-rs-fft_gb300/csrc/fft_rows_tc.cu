@@ -34,7 +34,7 @@ struct RowsTcCfg {
     static_assert(THREADS % 128 == 0, "one M = 128 MMA per 128 threads");
     static constexpr int NMMA = THREADS / 128;
     static constexpr uint32_t TMEM_COLS = rtc_tmem_cols(NMMA);
-    static constexpr size_t TILE_BYTES = (size_t)G * S::N * sizeof(float2);
+    static constexpr size_t TILE_BYTES = (size_t)G * rows_buf_stride<LOGN>() * sizeof(float2);
     static constexpr size_t A_BYTES = (size_t)THREADS * Gm::ROW_BYTES;
     static constexpr size_t A_ALL = Gm::PARTS * A_BYTES;
     // the A operand parts alias the exchange tile (tc_dft16 waits for its readers)

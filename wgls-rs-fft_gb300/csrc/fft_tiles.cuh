@@ -51,6 +51,17 @@ struct RowsChain<LOGN, I, LE, true> {
                                                Eng &) {}
 };
 
+// Samples between the exchange buffers of consecutive transforms of a rows
+// tile: N, plus T (one sample a thread) when a warp spans more than two
+// transforms (T < 16: N = 2^5 .. 2^7 with 16 samples a thread).  Unpadded, the
+// 32 / T buffers a warp touches would start on the same banks (16-, 8- and
+// 4-way conflicts); offset by 2T words each, one warp access covers 64
+// consecutive words: two wavefronts, the minimum for 32 8-byte lanes.
+template <int LOGN, int LE = 4>
+GBFFT_HD constexpr int rows_buf_stride() {
+    return SubCfg<LOGN, LE>::N + (SubCfg<LOGN, LE>::T < 16 ? SubCfg<LOGN, LE>::T : 0);
+}
+
 // Per-transform access for rows_tile: where transform g of the tile lives,
 // whether it exists, and its direction.
 struct RowRef {
@@ -62,7 +73,8 @@ struct RowRef {
 };
 
 // G transforms of length 2^LOGN; thread tid = g*T + t.  `ref(g)` gives the
-// transform's RowRef.  smem holds G*N complex values (unused if NSUB == 1).
+// transform's RowRef.  smem holds G * rows_buf_stride complex values (unused
+// if NSUB == 1).
 // DIRC: direction known at compile time (-1 forward: no sign or scale work at
 // all; +1 inverse: conjugate on load, RowRef's scales on store), or 0 (taken
 // from RowRef per transform, for launches that mix directions).
@@ -102,7 +114,7 @@ __device__ __forceinline__ void rows_tile(RefFn ref, const float2 *__restrict__ 
         }
     }
     subpass_run<LOGN, 0, LE>(v, t, tw, eng);
-    RowsChain<LOGN, 1, LE>::run(v, t, smem + g * C::N, tw, eng);
+    RowsChain<LOGN, 1, LE>::run(v, t, smem + g * rows_buf_stride<LOGN, LE>(), tw, eng);
     // last sub-pass (p R = N): output q of butterfly j sits at j + q p
     if (r.active) {
         constexpr int LR = C::logr(C::NSUB - 1), LP = C::logp(C::NSUB - 1);

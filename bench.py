@@ -50,6 +50,9 @@ WORKLOADS = {
     # name: (log2 N, batch, distribution, seed)
     "n4096_b16384": (12, 16384, "normal", 2),
     "n1024_b9": (10, 9, "uniform", 1),
+    "n32_b2097152": (5, 2097152, "normal", 2),
+    "n64_b1048576": (6, 1048576, "normal", 2),
+    "n128_b524288": (7, 524288, "normal", 2),
     "n256_b262144": (8, 262144, "normal", 2),
     "n512_b131072": (9, 131072, "normal", 2),
     "n1024_b65536": (10, 65536, "normal", 2),

@@ -188,6 +188,24 @@ def test_gpufft_mirror(lib_built):
     assert maxdiff(np.stack(rec), np.stack(x)) < 1e-5
     assert f.fft([]) == []
     assert f.benchmark_gpu_only(256, 64, warmup=1, iters=3) > 0
+    # the GPU-only timer agrees with CUDA events around the same in-place
+    # transforms on the caller's stream (within a factor of 1.5)
+    import torch
+    n, b, iters = 4096, 4096, 20
+    t_lib = f.benchmark_gpu_only(n, b, warmup=3, iters=iters)
+    d = torch.zeros(b, n, dtype=torch.complex64, device="cuda")
+    s = torch.cuda.current_stream()
+    ctx = f.context
+    for _ in range(3):
+        ctx.c2c_device(d, d, n, b, gbfft.FORWARD, stream=s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(iters):
+        ctx.c2c_device(d, d, n, b, gbfft.FORWARD, stream=s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    t_ev = e0.elapsed_time(e1) * 1e-3 / iters
+    assert t_ev / 1.5 <= t_lib <= t_ev * 1.5, (t_lib, t_ev)
     # the reference's errors and messages on both routes (equal lengths go
     # through the contiguous entry, unequal ones through the row entry)
     with pytest.raises(gbfft.GbfftError) as e:

@@ -19,43 +19,10 @@
 #include <algorithm>
 
 #include "gbfft_internal.h"
+#include "fft_rows.cuh"
 #include "fft_tiles.cuh"
 
 namespace gbfft {
-
-// LOGS: log2 of the samples one CTA moves (2^12 by default; 2^11 and 2^13 are
-// the autotuner's "transforms per CTA" alternatives for N <= 2^11).
-// LE: log2 of the samples a thread holds: 4, or 5 for N = 2^13 / 2^14, whose
-// radix-32 sub-passes (32 x 32 x 8, 32 x 32 x 16) need two exchanges instead
-// of three (16 x 16 x 16 x 2, 16 x 16 x 16 x 4) at 128 registers a thread.
-template <int LOGN, int LOGS = 12, int LE = 4>
-struct RowsCfg : SubCfg<LOGN, LE> {
-    using S = SubCfg<LOGN, LE>;
-    static constexpr int TILE = 1 << LOGS;
-    static constexpr int G_BY_SAMPLES = S::N >= TILE ? 1 : TILE / S::N;
-    static constexpr int G_BY_THREADS = S::T >= TILE / 16 ? 1 : (TILE / 16) / S::T;
-    static constexpr int G = G_BY_SAMPLES < G_BY_THREADS ? G_BY_SAMPLES : G_BY_THREADS;
-    static constexpr int THREADS = G * S::T;
-    static constexpr int REGS = LE == 4 ? 64 : 128;  // registers a thread
-    static constexpr int MINB = THREADS * REGS >= 65536 ? 1 : 65536 / (THREADS * REGS);
-    static constexpr size_t SMEM = S::NSUB > 1 ? (size_t)G * rows_buf_stride<LOGN, LE>() * sizeof(float2) : 0;
-};
-
-// DIRC: -1 forward, +1 inverse (a launch has one direction, so the sign and
-// scale work is resolved at compile time).
-template <int LOGN, int LOGS, int DIRC, int LE>
-__global__ void __launch_bounds__(RowsCfg<LOGN, LOGS, LE>::THREADS, RowsCfg<LOGN, LOGS, LE>::MINB)
-fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
-                float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
-    using C = RowsCfg<LOGN, LOGS, LE>;
-    extern __shared__ float2 smem_rows[];
-    auto ref = [&](int g) {
-        const uint64_t row = (uint64_t)blockIdx.x * C::G + g;
-        return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
-                      (uint32_t)row};
-    };
-    rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops);
-}
 
 // Persistent variant for the sizes whose per-transform footprint allows only
 // one or two CTAs per SM (N = 2^12 .. 2^14): each CTA walks tiles
@@ -65,7 +32,8 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
 template <int LOGN, int LOGS, int DIRC, int LE>
 __global__ void __launch_bounds__(RowsCfg<LOGN, LOGS, LE>::THREADS, RowsCfg<LOGN, LOGS, LE>::MINB)
 fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__restrict__ tw,
-                           float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops) {
+                           float in_im_sign, float out_re_scale, float out_im_scale, LoadOps ops,
+                           const uint64_t *, const uint64_t *) {  // (no row tables: the host never passes them)
     using C = RowsCfg<LOGN, LOGS, LE>;
     extern __shared__ float2 smem_rows[];
     constexpr uint32_t kTileSamples = C::G * C::N;
@@ -99,6 +67,7 @@ static void rows_describe(RowsKernelInfo &k) {
     k.fn_persistent = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, -1, LE>;
     k.fn_inv = (const void *)fft_rows_kernel<LOGN, LOGS, 1, LE>;
     k.fn_persistent_inv = (const void *)fft_rows_persistent_kernel<LOGN, LOGS, 1, LE>;
+    rows_tab_describe(LOGN, LOGS, LE, k);
     k.threads = C::THREADS;
     k.transforms_per_cta = C::G;
     k.smem = C::SMEM;
@@ -144,7 +113,8 @@ bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs, int loge) {
 cudaError_t rows_prepare(RowsKernelInfo &k) {
     cudaError_t e = cudaSuccess;
     if (k.smem > 48 * 1024) {
-        for (const void *fn : {k.fn, k.fn_persistent, k.fn_inv, k.fn_persistent_inv}) {
+        for (const void *fn : {k.fn, k.fn_persistent, k.fn_inv, k.fn_persistent_inv, k.fn_tab, k.fn_tab_inv}) {
+            if (!fn) continue;
             e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
             if (e != cudaSuccess) return e;
         }
@@ -159,12 +129,13 @@ cudaError_t rows_prepare(RowsKernelInfo &k) {
 
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
                         const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
-                        LoadOps ops) {
+                        LoadOps ops, const uint64_t *tab_in, const uint64_t *tab_out) {
     if (batch == 0) return cudaSuccess;
     uint64_t ctas = (batch + k.transforms_per_cta - 1) / k.transforms_per_cta;
     const bool inv = direction == GBFFT_INVERSE;
-    const void *fn = inv ? k.fn_inv : k.fn;
-    if (persistent && k.persist_ctas_per_sm > 0 && sms > 0) {
+    const void *fn = tab_in ? (inv ? k.fn_tab_inv : k.fn_tab) : (inv ? k.fn_inv : k.fn);
+    if (tab_in && !fn) return cudaErrorInvalidDeviceFunction;
+    if (persistent && k.persist_ctas_per_sm > 0 && sms > 0 && !tab_in) {
         fn = inv ? k.fn_persistent_inv : k.fn_persistent;
         ctas = std::min<uint64_t>(ctas, (uint64_t)k.persist_ctas_per_sm * (uint64_t)sms);
     }
@@ -172,8 +143,8 @@ cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, 
     const float scale = inv ? ldexpf(1.0f, -logn) : 1.0f;
     float in_im = inv ? -1.0f : 1.0f;
     float out_re = scale, out_im = inv ? -scale : 1.0f;
-    void *args[] = {(void *)&in, (void *)&out, (void *)&batch, (void *)&tw,
-                    (void *)&in_im, (void *)&out_re, (void *)&out_im, (void *)&ops};
+    void *args[] = {(void *)&in,     (void *)&out,    (void *)&batch, (void *)&tw,     (void *)&in_im,
+                    (void *)&out_re, (void *)&out_im, (void *)&ops,   (void *)&tab_in, (void *)&tab_out};
     return cudaLaunchKernel(fn, dim3((unsigned)ctas), dim3(k.threads), args, k.smem, stream);
 }
 

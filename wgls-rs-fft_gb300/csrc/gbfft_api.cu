@@ -518,21 +518,19 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
 
 // Host batch in pageable memory (contiguous at in_base/out_base, or separate
 // rows in_rows[r] / out_rows[r]) moved by the GPU through the host's page
-// tables: per chunk of whole transforms, one kernel gathers the chunk's rows
-// into HBM, the transform runs, one kernel scatters the result into the
-// caller's rows.  Chunks alternate over three streams so one chunk's gather,
-// another's transform and a third's scatter overlap.  Nothing runs on the host
-// but the launches; the call returns after the last chunk's scatter.
+// tables.  Single-pass sizes (FP32): one launch of the transform reads the
+// caller's rows and writes the caller's output rows directly.  Larger sizes
+// and the split forms: per chunk of whole transforms, one kernel gathers the
+// chunk's rows into HBM, the transform runs, one kernel scatters the result
+// into the caller's rows; chunks alternate over three streams so one chunk's
+// gather, another's transform and a third's scatter overlap.  Nothing runs on
+// the host but the launches; the call returns when the results are in place.
 static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, const char *in_base,
                                 char *out_base, const float *const *in_rows, float *const *out_rows) {
     const size_t row_bytes = (size_t)n * sizeof(float2);
     const size_t bytes = row_bytes * batch;
     const int logn = log2u(n);
-    int st = ctx->dbuf.ensure(bytes, ctx->err);
-    if (st == GBFFT_OK) st = ctx->dbuf_out.ensure(bytes, ctx->err);
-    if (st != GBFFT_OK) return st;
-    char *d = (char *)ctx->dbuf.ptr;
-    char *dy = (char *)ctx->dbuf_out.ptr;
+    int st = GBFFT_OK;
     const uint64_t *tin = nullptr, *tout = nullptr;
     uintptr_t align_bits = 0;
     if (in_rows && batch == 1) {  // one row: its own address is the base, no pointer table
@@ -570,6 +568,32 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     } else {
         align_bits = (uintptr_t)in_base | (uintptr_t)out_base;
     }
+    // Single-pass sizes in the FP32 form: the transform kernel itself reads the
+    // caller's rows and writes the results into the caller's output rows (one
+    // launch for the whole batch, no copy through HBM).  Its per-row layout is
+    // the plan's own, so results are the same bits as the other paths.
+    if (logn <= kRowsMaxLogN && ctx->precision == GBFFT_PREC_FP32) {
+        const PlanVariant v = choose_variant(ctx, logn, batch, direction, st);
+        Plan *plan = nullptr;
+        if (st == GBFFT_OK) st = get_plan(ctx, logn, v, &plan);
+        if (st != GBFFT_OK) return st;
+        if (!plan->multipass && (!tin || plan->rows.fn_tab)) {
+            const float *win = nullptr;
+            st = window_table(ctx, logn, &win);
+            if (st != GBFFT_OK) return st;
+            const LoadOps ops{win, ctx->noise_seed, ctx->noise_sigma, 0u};
+            GB_CUDA(ctx, rows_launch(plan->rows, (const float2 *)in_base, (float2 *)out_base, batch, plan->tw,
+                                     direction, logn, false, ctx->sms, ctx->xfer[0], ops, tin, tout));
+            ctx->launches += 1;
+            GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[0]));
+            return check_device_flag(ctx);
+        }
+    }
+    st = ctx->dbuf.ensure(bytes, ctx->err);
+    if (st == GBFFT_OK) st = ctx->dbuf_out.ensure(bytes, ctx->err);
+    if (st != GBFFT_OK) return st;
+    char *d = (char *)ctx->dbuf.ptr;
+    char *dy = (char *)ctx->dbuf_out.ptr;
     const bool vec16 = logn >= 1 && (align_bits & 15) == 0;
     uint64_t rows_per_chunk = row_bytes >= ctx->host_chunk ? 1 : ctx->host_chunk / row_bytes;
     if (logn > kRowsMaxLogN && rows_per_chunk < batch) {

@@ -38,6 +38,8 @@ struct RowsKernelInfo {
     const void *fn_persistent = nullptr;  // forward, tile loop with L2 prefetch of the next tile
     const void *fn_inv = nullptr;         // the same two for the inverse
     const void *fn_persistent_inv = nullptr;
+    const void *fn_tab = nullptr;         // forward / inverse over per-row address tables
+    const void *fn_tab_inv = nullptr;
     int persist_ctas_per_sm = 0;          // resident CTAs of fn_persistent (set by rows_prepare)
     int threads = 0;
     int transforms_per_cta = 0;
@@ -50,10 +52,15 @@ struct RowsKernelInfo {
 // loge: log2 of the samples a thread holds (4; 5 for N = 2^13, 2^14)
 bool rows_kernel_info(int logn, RowsKernelInfo &k, int logs = 12, int loge = 4);
 cudaError_t rows_prepare(RowsKernelInfo &k);
+// Sets fn_tab / fn_tab_inv for the tile (null where no table form is built).
+void rows_tab_describe(int logn, int logs, int loge, RowsKernelInfo &k);
 // persistent: use fn_persistent with at most persist_ctas_per_sm * sms CTAs.
+// tab_in / tab_out: device arrays of per-row addresses (row r read from
+// tab_in[r], written to tab_out[r]; in / out ignored); never persistent.
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
                         const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
-                        LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u});
+                        LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u}, const uint64_t *tab_in = nullptr,
+                        const uint64_t *tab_out = nullptr);
 
 // ---- host rows <-> device batch, copied by the GPU (host_rows.cu) ---------
 // Moves `rows` rows of 2^logn complex<f32> between caller host memory, reached

@@ -268,7 +268,27 @@ def run_reference_arm(args, workload):
     oracle.build()
     threads = os.cpu_count() or 1
     what = "reference Stockham R4/R2 f32 path restated in C"
-    if workload == "ragged_c5":
+    if workload == PIPELINE_WORKLOAD:
+        # the pipeline's stages on the host: noise (the shader's f32 arithmetic),
+        # forward transform, Hann window over the bins, inverse transform (1/N),
+        # one frame a step
+        n, batch = PIPELINE_N, PIPELINE_BATCH
+        frames = [pipeline_frame(f, n, batch) for f in range(4)]
+        w = signals.hann_window(n)[None, :]
+        state = {"f": 0}
+
+        def step():
+            f = state["f"]
+            x = frames[f % len(frames)] + oracle.ref_noise(batch, n, f, 0.1)
+            y = oracle.ref_fft(x, False, threads) * w
+            oracle.ref_fft(y, True, threads)
+            state["f"] = f + 1
+        samples = n * batch
+        sample = (f"one frame ({batch} rows of N={n}) per step: noise, forward, window, inverse; "
+                  f"{what}, {threads} threads")
+        data = "synthetic (the reference pipeline's sine frames)"
+        config = {"workload": workload, "n": n, "batch": batch, "slots": "n/a (host)", "l2": "n/a (host)"}
+    elif workload == "ragged_c5":
         # the whole ragged set every step (the same seeded transforms the GPU arm
         # runs), each (size, direction) group run as one batch
         descs, total = signals.ragged_set(args.ragged_count, seed=5)
@@ -466,6 +486,92 @@ def run_ragged(args, ctx, dev, rank, world):
 
 PRECISIONS = {"fp32": 0, "tc_fp16": 1, "tc_bf16x3": 2, "tc_tf32": 3, "tc_bf16x6": 4}
 
+# The reference's multi-slot pipeline (examples/parallel_pipeline.rs:738-742,
+# 109): N = 1024, batch 8, six slots in flight.
+PIPELINE_WORKLOAD = "pipeline_n1024_b8"
+PIPELINE_N, PIPELINE_BATCH, PIPELINE_SLOTS = 1024, 8, 6
+
+
+def pipeline_frame(seed, n, batch):
+    """The reference's test frame (parallel_pipeline.rs make_frame): row b,
+    sample i: sin(0.3 seed + 2 pi 5 t) + 0j with t = (b n + i) / n, in f32."""
+    import numpy as np
+    t = (np.arange(batch * n, dtype=np.float32) / np.float32(n)).reshape(batch, n)
+    arg = np.float32(seed) * np.float32(0.3) + t * np.float32(2 * np.pi) * np.float32(5.0)
+    return np.sin(arg).astype(np.complex64)
+
+
+def run_pipeline(args, dev, rank, world):
+    """One JSON line for the pipeline workload: host frames through six slots
+    (pinned staging, a stream each): host -> device copy, noise + forward
+    transform, window + inverse transform (1/N), device -> host copy.  One
+    step = one frame; the value is end to end (wall clock over the timed
+    frames, host copies included).  Device time of the two launches alone is
+    reported beside it."""
+    import numpy as np
+    import torch
+    from gbfft.pipeline import SpectralPipeline
+    n, batch, slots = PIPELINE_N, PIPELINE_BATCH, PIPELINE_SLOTS
+    frames = [pipeline_frame(f, n, batch) for f in range(args.steps + args.warmup)]
+    p = SpectralPipeline(n, batch, slots=slots, sigma=0.1, device=dev.index or 0)
+    p.run_frames(frames[:args.warmup])
+    torch.cuda.synchronize(dev)
+    l0 = p.fwd.launch_count() + p.inv.launch_count()
+    t0 = time.perf_counter()
+    outs = p.run_frames(frames[args.warmup:], seed_base=args.warmup)
+    el = max_over_ranks(time.perf_counter() - t0, dev)
+    launches = p.fwd.launch_count() + p.inv.launch_count() - l0
+    # device time of the two launches per frame, all slots' batches back to back
+    for i in range(slots):
+        p.inputs[i].copy_(torch.from_numpy(frames[i]))
+    p.run_eager()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    st = p.stream
+    e0.record(st)
+    reps = 20
+    for _ in range(reps):
+        p.run_eager()
+    e1.record(st)
+    torch.cuda.synchronize(dev)
+    dev_s = e0.elapsed_time(e1) * 1e-3 / (reps * slots)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    samples = n * batch
+    value = samples * args.steps * world / el / 1e9
+    peak, peak_kind = peaks()
+    alg = 2 * 16 * samples  # two single-pass transforms a frame
+    acc = None
+    try:
+        import oracle
+        acc = float(oracle.rel_l2(outs[0], oracle.ref_pipeline(frames[args.warmup], args.warmup, 0.1)))
+    except Exception:
+        pass
+    p.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (the reference pipeline's sine frames)",
+            "config": {"workload": PIPELINE_WORKLOAD, "n": n, "batch": batch, "slots": slots,
+                       "stages": "H2D, noise+FFT, window+IFFT(1/N), D2H", "l2": "n/a (64 KB frames)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": alg / dev_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": alg / dev_s / 1e9 / peak, "traffic": None, "peak_source": peak_kind,
+                         "accounting": "16 B/sample x 2 transforms a frame over the device time of the two launches",
+                         "launch_us": dev_s * 1e6 / 2},
+            "device_only": {"value": samples / dev_s / 1e9, "unit": UNIT,
+                            "api": "the two launches a frame, all slots back to back, CUDA events"},
+            "cpu_baseline": None,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 8 * samples, "d2h_bytes_per_step": 8 * samples,
+                    "api": "gbfft.pipeline.SpectralPipeline.run_frames (pinned staging, six slots)"},
+            "gpu_launches": launches,
+            "accuracy": {"rel_l2_vs_fp64": acc, "frame": args.warmup,
+                         "reference": "the pipeline in FP64 (checker only)"},
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
 
 def time_pairs(ctx, x, y, z, n, batch, steps, warmup, stream, dev, world=1):
     """Forward x -> y then inverse y -> z, `warmup` untimed and `steps` timed
@@ -616,7 +722,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ragged_c5"], default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ragged_c5", PIPELINE_WORKLOAD],
+                    default=DEFAULT_WORKLOAD)
     ap.add_argument("--precision", choices=sorted(PRECISIONS), default="fp32")
     ap.add_argument("--window", choices=["none", "hann"], default="none",
                     help="Hann window fused into every transform's load")
@@ -652,6 +759,9 @@ def main():
         rc = run_ragged(args, ctx, dev, rank, world)
         ctx.close()
         return rc
+    if workload == PIPELINE_WORKLOAD:
+        ctx.close()
+        return run_pipeline(args, dev, rank, world)
 
     logn, batch, distn, seed = WORKLOADS[workload]
     n = 1 << logn

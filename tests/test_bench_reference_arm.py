@@ -60,6 +60,9 @@ def test_reference_arm_uniform_and_ragged_workloads():
     _check_contract(line)
     assert line["config"]["workload"] == "ragged_c5" and line["config"]["transforms"] == 300
     assert "transforms" in line["cpu_baseline"]["sample"]
+    line = _run("--workload", "pipeline_n1024_b8")
+    _check_contract(line)
+    assert line["config"]["n"] == 1024 and line["config"]["batch"] == 8 and "window" in line["cpu_baseline"]["sample"]
 
 
 def test_reference_arm_under_torchrun_prints_once():

@@ -60,6 +60,25 @@ def test_pipeline_eager_and_graph(lib_built, oracle, torch, logn, batch):
     p.close()
 
 
+def test_pipeline_host_frames_six_slots(lib_built, oracle, torch):
+    """The reference's loop (examples/parallel_pipeline.rs:696-735): 14 host
+    frames of N = 1024 x 8 through six slots in flight, frame f with noise
+    seed f; every output against the FP64 pipeline, in frame order, and the
+    same bits as one frame through the pipeline on its own."""
+    from gbfft import signals
+    from gbfft.pipeline import SpectralPipeline
+    n, batch, nframes = 1024, 8, 14
+    frames = [signals.uniform_c64(batch, n, seed=100 + f) for f in range(nframes)]
+    p = SpectralPipeline(n, batch, slots=6, sigma=0.1)
+    outs = p.run_frames(frames)
+    assert len(outs) == nframes
+    for f, (x, y) in enumerate(zip(frames, outs)):
+        assert oracle.rel_l2(y, oracle.ref_pipeline(x, f, 0.1)) <= 2e-6, f
+    again = p.run_frames(frames[5:6], seed_base=5)
+    assert np.array_equal(again[0], outs[5])
+    p.close()
+
+
 def test_noise_argument_checks(lib_built):
     import gbfft
     with gbfft.Context(0) as ctx:

@@ -240,8 +240,8 @@ static void pass_describe(PassDesc &d, bool first) {
 }
 
 // First pass of 8 columns a CTA; tma: its input tile comes by the tensor
-// memory accelerator (32 samples a thread only), the LDG kernel kept as the
-// form for inputs that are not 16-byte aligned.
+// memory accelerator, the LDG kernel kept as the form for inputs that are not
+// 16-byte aligned.
 template <int LOGR, int LE>
 static void pass_describe_first8(PassDesc &d, bool tma) {
     using C = PassCfg<LOGR, LE, 3>;
@@ -252,17 +252,15 @@ static void pass_describe_first8(PassDesc &d, bool tma) {
     d.cols = C::COLS;
     d.nseg = subcfg_segments<LOGR, LE>(d.segs, 0);
     d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
-    if constexpr (LE == 5) {
-        if (tma) {
-            d.fn_tma = (const void *)fft_pass_first_tma_kernel<LOGR, LE>;
-            d.smem_tma = PassTmaCfg<LOGR, LE>::SMEM;
-        }
+    if (tma) {
+        d.fn_tma = (const void *)fft_pass_first_tma_kernel<LOGR, LE>;
+        d.smem_tma = PassTmaCfg<LOGR, LE>::SMEM;
     }
 }
 
 bool pass_kernel_info(int logr, bool first, PassDesc &d, int loge, int cols_log, bool tma) {
     d.logr = logr;
-    if (tma && !(first && cols_log == 3 && loge == 5)) return false;
+    if (tma && !(first && cols_log == 3)) return false;
     if (cols_log == 3) {  // first passes of radix 2^9 / 2^10 only
         if (!first) return false;
         switch (logr * 10 + loge) {

@@ -124,6 +124,7 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         if (e32) c.push_back(PlanVariant{10, true, true, 0, 5});
         c.push_back(PlanVariant{10, true, true});
         if (pass_kernel_info(logn - 16, true, pd, 4, 3)) c.push_back(PlanVariant{10, false, true, 3, 4});
+        if (pass_kernel_info(logn - 16, true, pd, 4, 3, true)) c.push_back(PlanVariant{10, false, true, 3, 4, true});
     }
     for (int m = top; m >= 7; --m) {
         const std::vector<int> parts = split_passes(logn, m);

@@ -206,14 +206,15 @@ def test_three_pass_first_pass_8_columns(tmp_path, monkeypatch, oracle, lib_buil
         assert oracle.rel_l2(outs[3][0], ref) <= TOL_REL_L2
 
 
-@pytest.mark.parametrize("loge", [5, 4])
+@pytest.mark.parametrize("loge,persistent", [(5, 0), (4, 0), (5, 1)])
 @pytest.mark.parametrize("logn,batch", [(25, 2), (26, 1)])
-def test_three_pass_first_pass_tma(tmp_path, monkeypatch, oracle, lib_built, logn, batch, loge):
+def test_three_pass_first_pass_tma(tmp_path, monkeypatch, oracle, lib_built, logn, batch, loge, persistent):
     """The 8-column first pass of N = 2^25 / 2^26 (32 or 16 samples a thread)
     with its input tile brought into shared memory by the tensor memory
     accelerator (tiled copies of a [256 rows][8 columns] box of a 3-D tensor
-    map; plan key "tma": 1) against the same pass with 8-byte loads
-    ("tma": 0): the same bits in both directions, and the FP64 gate."""
+    map; plan key "tma": 1; persistent: a tile loop that prefetches the next
+    tile's boxes into L2) against the same pass with 8-byte loads ("tma": 0):
+    the same bits in both directions, and the FP64 gate."""
     import numpy as np
 
     import gbfft
@@ -221,10 +222,10 @@ def test_three_pass_first_pass_tma(tmp_path, monkeypatch, oracle, lib_built, log
     x = signals.normal_c64(batch, 1 << logn, seed=1350 + logn)
     outs = {}
     for tma in (0, 1):
-        cache = tmp_path / f"tune_tma{tma}_{loge}.jsonl"
+        cache = tmp_path / f"tune_tma{tma}_{loge}_{persistent}.jsonl"
         lines = []
         for d in (gbfft.FORWARD, gbfft.INVERSE):
-            line = json.loads(_cache_line(logn, batch, d, 10, 0, tile=3, loge=loge))
+            line = json.loads(_cache_line(logn, batch, d, 10, persistent if tma else 0, tile=3, loge=loge))
             line["fused"] = 1
             line["tma"] = tma
             line["seconds"] = line.pop("seconds")  # key order as the library writes it

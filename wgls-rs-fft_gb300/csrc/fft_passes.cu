@@ -207,6 +207,93 @@ fft_pass_first_tma_kernel(const __grid_constant__ CUtensorMap map, float2 *out, 
     pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_pass);
 }
 
+__device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap *map, int x, int y, int z) {
+    asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"((uint64_t)map), "r"(x),
+                 "r"(y), "r"(z)
+                 : "memory");
+}
+
+// Persistent form: each CTA walks tiles blockIdx.x, +gridDim.x, ...; while a
+// tile is computed, the next tile's boxes are already being fetched into L2
+// (one TMA prefetch instruction a box), so its tiled copies find them there.
+// The mbarrier is re-armed every tile (phase = tile count & 1) after the CTA
+// barrier that ends the previous tile's reads of the shared tile.
+template <int LOGR, int LE>
+__global__ void __launch_bounds__(PassCfg<LOGR, LE, 3>::THREADS, PassCfg<LOGR, LE, 3>::MINB)
+fft_pass_first_tma_persistent_kernel(const __grid_constant__ CUtensorMap map, float2 *out, int logn,
+                                     const float2 *__restrict__ tw, const float2 *__restrict__ tw_lo,
+                                     const float2 *__restrict__ tw_hi, int tw_split, float in_im_sign, LoadOps ops,
+                                     uint32_t *err, uint64_t ntiles) {
+    using T = PassTmaCfg<LOGR, LE>;
+    constexpr int R = 1 << LOGR;
+    extern __shared__ __align__(1024) float2 smem_pass[];
+    uint64_t *bar = (uint64_t *)((char *)smem_pass + T::OFF_BAR);
+    int *s_fail = (int *)((char *)smem_pass + T::OFF_BAR + 8);
+    const int lognc = logn - LOGR;
+    const uint64_t per_row = 1ull << (lognc - 3);  // tiles a transform
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *s_fail = 0;
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, phase ^= 1u) {
+        const uint64_t b = tile / per_row;
+        const uint32_t col0 = (uint32_t)(tile % per_row) << 3;
+        if (threadIdx.x == 0) {
+            // the previous tile's shared-memory writes (exchanges, output staging)
+            // are ordered before the copies that overwrite the tile
+            fence_proxy_async_smem();
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                         "r"(T::TILE_BYTES)
+                         : "memory");
+#pragma unroll
+            for (int k = 0; k < R / kTmaBoxRows; ++k)
+                tma_load_3d(smem_u32(smem_pass + k * kTmaBoxRows * 8), &map, (int)(2 * col0), k * kTmaBoxRows,
+                            (int)b, smem_u32(bar));
+            const uint64_t next = tile + gridDim.x;
+            if (next < ntiles) {
+#pragma unroll
+                for (int k = 0; k < R / kTmaBoxRows; ++k)
+                    tma_prefetch_3d(&map, (int)(2 * ((uint32_t)(next % per_row) << 3)), k * kTmaBoxRows,
+                                    (int)(next / per_row));
+            }
+        }
+        uint32_t polls = 0;
+        bool done = mbar_try_wait(bar, phase);
+        while (!done && ++polls < kTmaSpinLimit) done = mbar_try_wait(bar, phase);
+        if (!done) *s_fail = 1;
+        __syncthreads();
+        if (*s_fail) {
+            if (threadIdx.x == 0) {
+                atomicExch(err, 4u);
+                for (uint32_t n = 0; n < kTmaSpinLimit && !mbar_try_wait(bar, phase); ++n) {
+                }
+            }
+            __syncthreads();
+            return;
+        }
+        PassArgs a;
+        a.src = nullptr;
+        a.dst = out + (b << logn);
+        a.logn = logn;
+        a.logp = 0;
+        a.col0 = col0;
+        a.tw_sub = tw;
+        a.tw_lo = tw_lo;
+        a.tw_hi = tw_hi;
+        a.tw_split = tw_split;
+        a.in_im = in_im_sign;
+        a.out_re = 1.0f;
+        a.out_im = 1.0f;
+        a.coherent_load = false;
+        a.row = (uint32_t)b;
+        a.ops = ops;
+        pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_pass);
+        __syncthreads();  // every read of the shared tile is done before the next tile's copies
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -254,6 +341,7 @@ static void pass_describe_first8(PassDesc &d, bool tma) {
     d.tw_entries = SubCfg<LOGR, LE>::tw_entries();
     if (tma) {
         d.fn_tma = (const void *)fft_pass_first_tma_kernel<LOGR, LE>;
+        d.fn_tma_persistent = (const void *)fft_pass_first_tma_persistent_kernel<LOGR, LE>;
         d.smem_tma = PassTmaCfg<LOGR, LE>::SMEM;
     }
 }
@@ -295,6 +383,14 @@ cudaError_t pass_prepare(PassDesc &d) {
     cudaError_t e = cudaSuccess;
     if (d.fn_tma && d.smem_tma > 48 * 1024) {
         e = cudaFuncSetAttribute(d.fn_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)d.smem_tma);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(d.fn_tma_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)d.smem_tma);
+        if (e != cudaSuccess) return e;
+    }
+    if (d.fn_tma_persistent) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.tma_ctas_per_sm, d.fn_tma_persistent, d.threads,
+                                                          d.smem_tma);
         if (e != cudaSuccess) return e;
     }
     if (d.smem > 48 * 1024) {
@@ -331,6 +427,14 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
         if (encode(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)in, dims, strides, box, estr,
                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+            if (persistent && d.fn_tma_persistent && d.tma_ctas_per_sm > 0 && sms > 0) {
+                const uint64_t grid = std::min<uint64_t>(tiles, (uint64_t)d.tma_ctas_per_sm * (uint64_t)sms);
+                void *pargs[] = {(void *)&map,   (void *)&out,      (void *)&logn,       (void *)&tw_sub,
+                                 (void *)&tw_lo, (void *)&tw_hi,    (void *)&tw_split,   (void *)&in_im_sign,
+                                 (void *)&ops,   (void *)&err,      (void *)&tiles};
+                return cudaLaunchKernel(d.fn_tma_persistent, dim3((unsigned)grid), dim3(d.threads), pargs,
+                                        d.smem_tma, stream);
+            }
             void *args[] = {(void *)&map,  (void *)&out,   (void *)&logn,     (void *)&tw_sub,     (void *)&tw_lo,
                             (void *)&tw_hi, (void *)&tw_split, (void *)&in_im_sign, (void *)&ops, (void *)&err};
             return cudaLaunchKernel(d.fn_tma, dim3((unsigned)tiles), dim3(d.threads), args, d.smem_tma, stream);

@@ -116,7 +116,10 @@ std::vector<PlanVariant> plan_candidates(int logn, int precision) {
         const bool e32 = pass_kernel_info(logn - 16, true, pd, 5);
         // its 8-column input tile brought in by the TMA (four tiled copies a
         // tile instead of 32 8-byte loads a thread)
-        if (pass_kernel_info(logn - 16, true, pd, 5, 3, true)) c.push_back(PlanVariant{10, false, true, 3, 5, true});
+        if (pass_kernel_info(logn - 16, true, pd, 5, 3, true)) {
+            c.push_back(PlanVariant{10, false, true, 3, 5, true});
+            c.push_back(PlanVariant{10, true, true, 3, 5, true});  // persistent, next tile prefetched to L2
+        }
         if (pass_kernel_info(logn - 16, true, pd, 5, 3)) c.push_back(PlanVariant{10, false, true, 3, 5});
         if (e32) c.push_back(PlanVariant{10, false, true, 0, 5});
         c.push_back(PlanVariant{10, false, true});

@@ -35,6 +35,8 @@ struct PassDesc {
     int tw_entries = 0;
     bool tc = false;                    // radix-16 butterflies on the tensor cores
     const void *fn_tma = nullptr;       // first pass with its input tile brought in by the TMA
+    const void *fn_tma_persistent = nullptr;  // the same as a tile loop prefetching the next tile into L2
+    int tma_ctas_per_sm = 0;
     size_t smem_tma = 0;
 };
 

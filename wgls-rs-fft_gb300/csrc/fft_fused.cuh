@@ -77,6 +77,12 @@ struct FusedParams {
     uint32_t *err;
     uint32_t spin_limit;
     const uint4 *gtab;  // split forms: the G operand table (fft_passes_tc.cu)
+    // Two-pass transforms only: when set, pass A reads transform b from
+    // tab_in[b] and pass B writes it to tab_out[b] (the addresses of the
+    // caller's host rows, which the GPU reaches through the host's page
+    // tables); `out` then holds only the intermediate.  Null otherwise.
+    const uint64_t *tab_in;
+    const uint64_t *tab_out;
 };
 
 __device__ __forceinline__ uint32_t fused_ld_acquire(const uint32_t *p) {
@@ -150,7 +156,7 @@ __device__ __forceinline__ void fused_loop(const FusedParams &P, float2 *smem_f,
         a.tw_split = (LOGN + 1) / 2;
         a.row = b;
         if (is_a) {
-            a.src = P.in + base;
+            a.src = (C::FIRST_A && P.tab_in) ? (const float2 *)P.tab_in[b] : P.in + base;
             a.dst = P.out + base;
             a.logp = LOGPA;
             // two passes: tiles in column order; last two of three: column
@@ -181,7 +187,7 @@ __device__ __forceinline__ void fused_loop(const FusedParams &P, float2 *smem_f,
             __syncthreads();
             if (s_abort) break;
             a.src = P.out + base;
-            a.dst = P.out + base;
+            a.dst = (C::FIRST_A && P.tab_out) ? (float2 *)P.tab_out[b] : P.out + base;
             a.logp = C::LOGPB;
             a.col0 = C::FIRST_A ? tile * (uint32_t)(kCols * C::NGB) : (tile * GPT + g) * (uint32_t)kCols;
             a.tw_sub = P.tw_b;

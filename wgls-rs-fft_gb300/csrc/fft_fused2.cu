@@ -92,8 +92,10 @@ uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms) {
 cudaError_t fused_launch(const FusedDesc &d, const float2 *in, float2 *out, uint64_t batch, const float2 *tw_a,
                          const float2 *tw_b, const float2 *tw_lo, const float2 *tw_hi, float in_im, float out_re,
                          float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream,
-                         const void *gtab) {
+                         const void *gtab, const uint64_t *tab_in, const uint64_t *tab_out) {
     FusedParams P;
+    P.tab_in = tab_in;
+    P.tab_out = tab_out;
     P.in = in;
     P.out = out;
     P.batch = (uint32_t)batch;

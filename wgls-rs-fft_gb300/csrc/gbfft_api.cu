@@ -531,14 +531,24 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     const size_t bytes = row_bytes * batch;
     const int logn = log2u(n);
     int st = GBFFT_OK;
-    const uint64_t *tin = nullptr, *tout = nullptr;
-    uintptr_t align_bits = 0;
-    if (in_rows && batch == 1) {  // one row: its own address is the base, no pointer table
+    // the plan the device entry would run for this shape decides the route
+    const PlanVariant v0 = choose_variant(ctx, logn, batch, direction, st);
+    Plan *plan = nullptr;
+    if (st == GBFFT_OK) st = get_plan(ctx, logn, v0, &plan);
+    if (st != GBFFT_OK) return st;
+    // single-pass FP32: the transform kernel reads and writes the caller's rows;
+    // a fused two-pass plan: its first pass reads them, its second writes them
+    const bool single = !plan->multipass && ctx->precision == GBFFT_PREC_FP32;
+    const bool pair = plan->has_fused && plan->passes.size() == 2 &&
+                      batch * plan->fused.groups_per_transform <= 0x7fffffffull;
+    if (in_rows && batch == 1 && !pair) {  // one row: its own address is the base, no pointer table
         in_base = (const char *)in_rows[0];
         out_base = (char *)out_rows[0];
         in_rows = nullptr;
     }
-    if (in_rows) {
+    const uint64_t *tin = nullptr, *tout = nullptr;
+    uintptr_t align_bits = 0;
+    if (in_rows || pair) {  // row addresses as device tables (the fused pair reads rows through them only)
         const size_t tbytes = 2 * batch * sizeof(uint64_t);
         if (ctx->htable_bytes < tbytes) {
             if (ctx->htable) cudaFreeHost(ctx->htable);
@@ -555,9 +565,11 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
         st = ctx->dtable.ensure(tbytes, ctx->err);
         if (st != GBFFT_OK) return st;
         for (uint64_t r = 0; r < batch; ++r) {
-            ctx->htable[r] = (uint64_t)(uintptr_t)in_rows[r];
-            ctx->htable[batch + r] = (uint64_t)(uintptr_t)out_rows[r];
-            align_bits |= (uintptr_t)in_rows[r] | (uintptr_t)out_rows[r];
+            const uintptr_t a = in_rows ? (uintptr_t)in_rows[r] : (uintptr_t)(in_base + r * row_bytes);
+            const uintptr_t b = in_rows ? (uintptr_t)out_rows[r] : (uintptr_t)(out_base + r * row_bytes);
+            ctx->htable[r] = (uint64_t)a;
+            ctx->htable[batch + r] = (uint64_t)b;
+            align_bits |= a | b;
         }
         GB_CUDA(ctx, cudaMemcpyAsync(ctx->dtable.ptr, ctx->htable, tbytes, cudaMemcpyHostToDevice, ctx->xfer[0]));
         GB_CUDA(ctx, cudaEventRecord(ctx->ev_table, ctx->xfer[0]));
@@ -568,26 +580,42 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     } else {
         align_bits = (uintptr_t)in_base | (uintptr_t)out_base;
     }
-    // Single-pass sizes in the FP32 form: the transform kernel itself reads the
-    // caller's rows and writes the results into the caller's output rows (one
-    // launch for the whole batch, no copy through HBM).  Its per-row layout is
-    // the plan's own, so results are the same bits as the other paths.
-    if (logn <= kRowsMaxLogN && ctx->precision == GBFFT_PREC_FP32) {
-        const PlanVariant v = choose_variant(ctx, logn, batch, direction, st);
-        Plan *plan = nullptr;
-        if (st == GBFFT_OK) st = get_plan(ctx, logn, v, &plan);
+    if (single && (!tin || plan->rows.fn_tab)) {
+        // one launch for the whole batch, no copy through HBM; the plan's own
+        // per-row layout, so the same bits as the other paths
+        const float *win = nullptr;
+        st = window_table(ctx, logn, &win);
         if (st != GBFFT_OK) return st;
-        if (!plan->multipass && (!tin || plan->rows.fn_tab)) {
-            const float *win = nullptr;
-            st = window_table(ctx, logn, &win);
-            if (st != GBFFT_OK) return st;
-            const LoadOps ops{win, ctx->noise_seed, ctx->noise_sigma, 0u};
-            GB_CUDA(ctx, rows_launch(plan->rows, (const float2 *)in_base, (float2 *)out_base, batch, plan->tw,
-                                     direction, logn, false, ctx->sms, ctx->xfer[0], ops, tin, tout));
-            ctx->launches += 1;
-            GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[0]));
-            return check_device_flag(ctx);
-        }
+        const LoadOps ops{win, ctx->noise_seed, ctx->noise_sigma, 0u};
+        GB_CUDA(ctx, rows_launch(plan->rows, (const float2 *)in_base, (float2 *)out_base, batch, plan->tw,
+                                 direction, logn, false, ctx->sms, ctx->xfer[0], ops, tin, tout));
+        ctx->launches += 1;
+        GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[0]));
+        return check_device_flag(ctx);
+    }
+    if (pair) {
+        // one launch of the fused pair: pass A reads the caller's rows, the
+        // intermediate stays in device memory (mostly L2), pass B writes the
+        // caller's output rows
+        st = ctx->dbuf_out.ensure(bytes, ctx->err);
+        if (st != GBFFT_OK) return st;
+        const float *win = nullptr;
+        st = window_table(ctx, logn, &win);
+        if (st != GBFFT_OK) return st;
+        const LoadOps ops{win, ctx->noise_seed, ctx->noise_sigma, 0u};
+        std::unique_ptr<DeviceBuffer> &cb = ctx->fused_ctr[ctx->xfer[0]];
+        if (!cb) cb.reset(new DeviceBuffer());
+        ctx->err_armed = true;
+        uint64_t launches = 0;
+        std::string why;
+        st = plan_execute_tables(*plan, tin, tout, (float2 *)ctx->dbuf_out.ptr, batch, direction, ctx->d_err,
+                                 ctx->xfer[0], launches, why, ops, cb.get());
+        ctx->launches += launches;
+        if (st != GBFFT_OK)
+            return fail(ctx, st, "execute N=%llu batch=%llu: %s", (unsigned long long)n, (unsigned long long)batch,
+                        why.c_str());
+        GB_CUDA(ctx, cudaStreamSynchronize(ctx->xfer[0]));
+        return check_device_flag(ctx);
     }
     st = ctx->dbuf.ensure(bytes, ctx->err);
     if (st == GBFFT_OK) st = ctx->dbuf_out.ensure(bytes, ctx->err);

@@ -282,6 +282,42 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
     return GBFFT_OK;
 }
 
+int plan_execute_tables(const Plan &p, const uint64_t *tab_in, const uint64_t *tab_out, float2 *work,
+                        uint64_t batch, int direction, uint32_t *err, cudaStream_t stream, uint64_t &launches,
+                        std::string &why, LoadOps ops, DeviceBuffer *ctr) {
+    launches = 0;
+    if (batch == 0) return GBFFT_OK;
+    if (!p.has_fused || p.passes.size() != 2 || !ctr || batch * p.fused.groups_per_transform > 0x7fffffffull) {
+        why = "row tables need a fused two-pass plan";
+        return GBFFT_ERR_UNSUPPORTED;
+    }
+    cudaError_t e;
+    const uint64_t ngroups = batch * p.fused.groups_per_transform;
+    const size_t want = (2 + (size_t)ngroups) * sizeof(uint32_t);
+    if (ctr->bytes < want) {
+        int st = ctr->ensure(want, why);
+        if (st != GBFFT_OK) return st;
+        // the kernel leaves the block zeroed; a new block starts zeroed
+        if ((e = cudaMemsetAsync(ctr->ptr, 0, ctr->bytes, stream)) != cudaSuccess) {
+            why = cudaGetErrorString(e);
+            return GBFFT_ERR_CUDA;
+        }
+    }
+    const bool inv = direction == GBFFT_INVERSE;
+    const float scale = inv ? ldexpf(1.0f, -p.logn) : 1.0f;
+    const float2 *tw_a = p.fused.sub_off_a >= 0 ? p.tw + p.fused.sub_off_a : p.tw + p.passes[0].sub_tw_offset;
+    const float2 *tw_b = p.fused.sub_off_b >= 0 ? p.tw + p.fused.sub_off_b : p.tw + p.passes[1].sub_tw_offset;
+    e = fused_launch(p.fused, nullptr, work, batch, tw_a, tw_b, p.tw + p.tw_lo_offset, p.tw + p.tw_hi_offset,
+                     inv ? -1.0f : 1.0f, scale, inv ? -scale : 1.0f, ops, (uint32_t *)ctr->ptr, err, p.sms, stream,
+                     p.gtab, tab_in, tab_out);
+    if (e != cudaSuccess) {
+        why = cudaGetErrorString(e);
+        return GBFFT_ERR_CUDA;
+    }
+    launches = 1;
+    return GBFFT_OK;
+}
+
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction, DeviceBuffer &ws,
                  uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why, LoadOps ops,
                  DeviceBuffer *ctr) {

@@ -154,7 +154,8 @@ uint32_t fused_lag(const FusedDesc &d, uint64_t ngroups, int sms);
 cudaError_t fused_launch(const FusedDesc &d, const float2 *in, float2 *out, uint64_t batch, const float2 *tw_a,
                          const float2 *tw_b, const float2 *tw_lo, const float2 *tw_hi, float in_im, float out_re,
                          float out_im, LoadOps ops, uint32_t *ctr, uint32_t *err, int sms, cudaStream_t stream,
-                         const void *gtab = nullptr);
+                         const void *gtab = nullptr, const uint64_t *tab_in = nullptr,
+                         const uint64_t *tab_out = nullptr);
 
 // log2 radices (each <= max_logr) of the global passes for a multi-pass
 // transform of 2^logn.
@@ -180,5 +181,14 @@ int plan_build(Plan &p, int logn, int precision, const PlanVariant &v, cudaStrea
 int plan_execute(const Plan &p, const float2 *in, float2 *out, uint64_t batch, int direction,
                  DeviceBuffer &ws, uint32_t *err, cudaStream_t stream, uint64_t &launches, std::string &why,
                  LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u}, DeviceBuffer *ctr = nullptr);
+
+// A two-pass fused plan (has_fused, two passes) over the caller's rows: pass
+// A reads transform b from tab_in[b] and pass B writes it to tab_out[b]
+// (device arrays of row addresses the GPU reaches through the host's page
+// tables); `work` (batch << logn samples of device memory) holds the
+// intermediate.  One launch.
+int plan_execute_tables(const Plan &p, const uint64_t *tab_in, const uint64_t *tab_out, float2 *work,
+                        uint64_t batch, int direction, uint32_t *err, cudaStream_t stream, uint64_t &launches,
+                        std::string &why, LoadOps ops, DeviceBuffer *ctr);
 
 }  // namespace gbfft

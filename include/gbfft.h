@@ -249,6 +249,10 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
  *   GBFFT_HOST_PATH=staged                 pageable host batches go through pinned
  *                                          staging even where the GPU could reach
  *                                          them directly
+ *   GBFFT_HOST_PATH=gather                 the GPU copies pageable rows into device
+ *                                          memory and back around every transform
+ *                                          instead of the transform reading and
+ *                                          writing them itself
  *   GBFFT_DEVICE_ALLOC_CAP=<bytes>         device requests above it fail with
  *                                          GBFFT_ERR_OUT_OF_MEMORY (tests the
  *                                          out-of-memory paths without a real one) */

@@ -126,6 +126,7 @@ struct gbfft_ctx {
     // the host's page tables when the device can (cudaDevAttrPageableMemoryAccess;
     // GBFFT_HOST_PATH=staged turns it off): no host memcpy, no pinned staging.
     bool host_direct = false;
+    bool host_gather = false;  // GBFFT_HOST_PATH=gather: copy kernels around every transform
     int sms = 0;
     DeviceBuffer dtable;          // device copy of the caller's row pointers (in, then out)
     uint64_t *htable = nullptr;   // its pinned source
@@ -538,8 +539,8 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     if (st != GBFFT_OK) return st;
     // single-pass FP32: the transform kernel reads and writes the caller's rows;
     // a fused two-pass plan: its first pass reads them, its second writes them
-    const bool single = !plan->multipass && ctx->precision == GBFFT_PREC_FP32;
-    const bool pair = plan->has_fused && plan->passes.size() == 2 &&
+    const bool single = !ctx->host_gather && !plan->multipass && ctx->precision == GBFFT_PREC_FP32;
+    const bool pair = !ctx->host_gather && plan->has_fused && plan->passes.size() == 2 &&
                       batch * plan->fused.groups_per_transform <= 0x7fffffffull;
     if (in_rows && batch == 1 && !pair) {  // one row: its own address is the base, no pointer table
         in_base = (const char *)in_rows[0];
@@ -724,6 +725,7 @@ int gbfft_create(int device, gbfft_ctx **out_ctx) {
     }
     const char *hp = getenv("GBFFT_HOST_PATH");
     ctx->host_direct = pageable == 1 && !(hp && !strcmp(hp, "staged"));
+    ctx->host_gather = hp && !strcmp(hp, "gather");
     if (const char *a = getenv("GBFFT_AUTOTUNE")) ctx->auto_tune = a[0] == '1';
     if (const char *a = getenv("GBFFT_AUTOTUNE_VERBOSE")) ctx->tune_verbose = a[0] == '1';
     *out_ctx = ctx.release();

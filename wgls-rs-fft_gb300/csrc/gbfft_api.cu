@@ -526,8 +526,12 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
 // into the caller's rows; chunks alternate over three streams so one chunk's
 // gather, another's transform and a third's scatter overlap.  Nothing runs on
 // the host but the launches; the call returns when the results are in place.
+// kNotDirect: returned (before any work) when allow_gather is false and the
+// shape would need the gather / scatter route, so the caller takes its own.
+constexpr int kNotDirect = -1;
 static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, const char *in_base,
-                                char *out_base, const float *const *in_rows, float *const *out_rows) {
+                                char *out_base, const float *const *in_rows, float *const *out_rows,
+                                bool allow_gather = true) {
     const size_t row_bytes = (size_t)n * sizeof(float2);
     const size_t bytes = row_bytes * batch;
     const int logn = log2u(n);
@@ -542,6 +546,7 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     const bool single = !ctx->host_gather && !plan->multipass && ctx->precision == GBFFT_PREC_FP32;
     const bool pair = !ctx->host_gather && plan->has_fused && plan->passes.size() == 2 &&
                       batch * plan->fused.groups_per_transform <= 0x7fffffffull;
+    if (!allow_gather && !(single && !in_rows) && !pair) return kNotDirect;
     if (in_rows && batch == 1 && !pair) {  // one row: its own address is the base, no pointer table
         in_base = (const char *)in_rows[0];
         out_base = (char *)out_rows[0];
@@ -809,8 +814,14 @@ static int host_contiguous(gbfft_ctx *ctx, const float *in, float *out, uint64_t
                            int direction) {
     const size_t row_bytes = (size_t)n * sizeof(float2);
     const bool pinned = host_is_pinned(in) && host_is_pinned(out);
-    if (!pinned && ctx->host_direct)
-        return host_pipeline_direct(ctx, n, batch, direction, (const char *)in, (char *)out, nullptr, nullptr);
+    if (ctx->host_direct) {
+        // pinned batches too go straight through the transform kernels where
+        // those read and write host memory themselves; otherwise the copy
+        // engines move them (faster than copy kernels for pinned memory)
+        const int st = host_pipeline_direct(ctx, n, batch, direction, (const char *)in, (char *)out, nullptr,
+                                            nullptr, !pinned);
+        if (st != kNotDirect) return st;
+    }
     auto in_row = [&](uint64_t r) { return (const char *)in + r * row_bytes; };
     auto out_row = [&](uint64_t r) { return (char *)out + r * row_bytes; };
     return host_pipeline(ctx, n, batch, direction, pinned ? in : nullptr, pinned ? out : nullptr, in_row, out_row);

@@ -309,3 +309,29 @@ def test_autotune_split_form(tmp_path, monkeypatch, oracle, lib_built, prec, tol
     assert oracle.rel_l2(y, oracle.fft64(x)) <= tol
     lines = [json.loads(l) for l in cache.read_text().splitlines()]
     assert len(lines) == 1 and lines[0]["precision"] == prec and lines[0]["logn"] == 16
+
+
+@pytest.mark.parametrize("logn,batch", [(6, 40), (8, 37), (10, 9), (12, 5), (13, 3), (14, 2)])
+def test_packed_and_scalar_butterflies_same_bits(tmp_path, monkeypatch, oracle, lib_built, logn, batch):
+    """The single-pass kernel runs its butterflies and twiddles with packed
+    two-lane FP32 instructions from N = 2^8, the persistent tile loop with
+    scalar ones; each lane of a packed add, subtract, FMA or multiply rounds
+    like the scalar operation, so both give the same bits in both directions
+    (and meet the FP64 gate)."""
+    import numpy as np
+
+    import gbfft
+    from gbfft import signals
+    x = signals.normal_c64(batch, 1 << logn, seed=1400 + logn)
+    outs = {}
+    for persistent in (0, 1):
+        cache = tmp_path / f"tune_p{persistent}.jsonl"
+        cache.write_text("\n".join(_cache_line(logn, batch, d, 10, persistent, loge=4)
+                                   for d in (gbfft.FORWARD, gbfft.INVERSE)) + "\n")
+        monkeypatch.setenv("GBFFT_AUTOTUNE_CACHE", str(cache))
+        with gbfft.Context(0) as ctx:
+            outs[persistent] = [ctx.c2c_host(x, d) for d in (gbfft.FORWARD, gbfft.INVERSE)]
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    for y, inv in zip(outs[0], (False, True)):
+        assert oracle.rel_l2(y, oracle.fft64(x, inverse=inv)) <= TOL_REL_L2

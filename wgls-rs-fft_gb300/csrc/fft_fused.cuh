@@ -231,7 +231,11 @@ template <int LOGRA, int LOGRB, int THREADS, int LOGN, int LOGPA, int LE = 4>
 __global__ void __launch_bounds__(THREADS, (FusedCfg<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>::MINB))
 fft_fused_kernel(FusedParams P) {
     extern __shared__ float2 smem_f[];
-    fused_loop<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>(P, smem_f, DftRegs());
+    // packed FP32 butterflies (2^16: 226 -> 232 GSa/s), except for pairs with a
+    // radix-2^10 pass (32 x 32 sub-passes at 128 registers), where the scalar
+    // ones measured faster (2^19: 152.4 against 149.8 GSa/s)
+    using Eng = std::conditional_t<(LOGRA >= 10 || LOGRB >= 10), DftRegsScalar, DftRegs>;
+    fused_loop<LOGRA, LOGRB, THREADS, LOGN, LOGPA, LE>(P, smem_f, Eng{});
     fused_finish<THREADS>(P);
 }
 

@@ -51,7 +51,9 @@ fft_rows_persistent_kernel(const float2 *in, float2 *out, uint64_t batch, const 
             return RowRef{in + row * C::N, out + row * C::N, row < batch, in_im_sign, out_re_scale, out_im_scale,
                       (uint32_t)row};
         };
-        rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops);
+        // scalar butterflies: this loop serves N = 2^14, one transform per SM,
+        // where the packed ones measured slower (276 against 259 GSa/s)
+        rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops, DftRegsScalar{});
         __syncthreads();  // shared memory is reused by the next tile
     }
 }

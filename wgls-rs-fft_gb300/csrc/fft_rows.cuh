@@ -50,7 +50,11 @@ fft_rows_kernel(const float2 *in, float2 *out, uint64_t batch, const float2 *__r
                           (uint32_t)row};
         }
     };
-    rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops);
+    // packed FP32 butterflies and twiddles from N = 2^8 (N = 4096: 401 -> 419
+    // GSa/s); scalar below, where several transforms share a warp (2^6: 406
+    // scalar against 399 packed)
+    using Eng = std::conditional_t<(LOGN >= 8), DftRegsX2, DftRegsScalar>;
+    rows_tile<LOGN, C::G, DIRC, LE>(ref, tw, smem_rows, ops, Eng{});
 }
 
 }  // namespace gbfft

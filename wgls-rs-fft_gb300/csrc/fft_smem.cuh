@@ -12,6 +12,7 @@
 // sub-pass of radix R it runs E/R butterflies j = t + T b, butterfly b using
 // register slots b + m E/R.
 #pragma once
+#include <type_traits>
 #include <utility>
 
 #include "fft_core.cuh"
@@ -94,18 +95,19 @@ GBFFT_HD float2 mul_w32c(float2 a) {
 
 // 32-point DFT: radix-2 decimation in frequency, then two 16-point DFTs.
 template <> struct Dft<32> {
+    template <bool PK = true>
     GBFFT_HD static void run(float2 *x) {
         float2 a[16], b[16];
         auto split = [&](auto kc) {
             constexpr int k = decltype(kc)::value;
-            a[k] = cadd(x[k], x[k + 16]);
-            b[k] = mul_w32c<k>(csub(x[k], x[k + 16]));
+            a[k] = cadd<PK>(x[k], x[k + 16]);
+            b[k] = mul_w32c<k>(csub<PK>(x[k], x[k + 16]));
         };
         [&]<int... Ks>(std::integer_sequence<int, Ks...>) {
             (split(std::integral_constant<int, Ks>{}), ...);
         }(std::make_integer_sequence<int, 16>{});
-        Dft<16>::run(a);
-        Dft<16>::run(b);
+        Dft<16>::run<PK>(a);
+        Dft<16>::run<PK>(b);
         GBFFT_UNROLL
         for (int k = 0; k < 16; ++k) {
             x[2 * k] = a[k];
@@ -120,12 +122,26 @@ struct FactoredTw {
     static constexpr int idx32 = ((M * B) << (5 - LOGE)) & 31;
 };
 
-// Engine of the radix-R butterflies: FP32 in registers (DftRegs) or, for the
-// split-precision form, tensor-core matrix products (fft_tc.cuh).
-struct DftRegs {
+// Engine of the radix-R butterflies: FP32 in registers (DftRegs, packed
+// two-lane adds; DftRegsScalar, scalar ones) or, for the split-precision form,
+// tensor-core matrix products (fft_tc.cuh).
+template <bool PK>
+struct DftRegsT {
     template <int R>
-    __device__ __forceinline__ void run(float2 (&x)[R]) { Dft<R>::run(x); }
+    __device__ __forceinline__ void run(float2 (&x)[R]) { Dft<R>::template run<PK>(x); }
 };
+using DftRegs = DftRegsT<true>;
+using DftRegsScalar = DftRegsT<false>;
+// The same butterflies, with the sub-pass twiddles applied by the packed
+// complex multiply (cmul_x2: same bits, faster in the single-pass kernel).
+struct DftRegsX2 : DftRegs {};
+
+// a * twiddle b in the way the engine prefers
+template <class Eng>
+__device__ __forceinline__ float2 twiddle_mul(float2 a, float2 b) {
+    if constexpr (std::is_same_v<Eng, DftRegsX2>) return cmul_x2(a, b);
+    else return cmul(a, b);
+}
 
 // Butterflies of one sub-pass on the register array v.
 template <int LOGE, int LOGR, int LOGP, int LOGT, bool FACT = false, class Eng = DftRegs>
@@ -142,7 +158,8 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
             for (int m = 0; m < R; ++m) x[m] = v[b + m * NB];
             auto apply = [&](auto mc) {
                 constexpr int M = decltype(mc)::value;
-                if constexpr (M > 0) x[M] = cmul(mul_w32c<FactoredTw<LOGE, LOGR, b, M>::idx32>(x[M]), wt[M]);
+                if constexpr (M > 0)
+                    x[M] = twiddle_mul<Eng>(mul_w32c<FactoredTw<LOGE, LOGR, b, M>::idx32>(x[M]), wt[M]);
             };
             [&]<int... Ms>(std::integer_sequence<int, Ms...>) {
                 (apply(std::integral_constant<int, Ms>{}), ...);
@@ -164,7 +181,7 @@ __device__ __forceinline__ void subpass_compute(float2 (&v)[1 << LOGE], int t, c
                 const int j = t + T * b;
                 const int k = j & (P - 1);
 #pragma unroll
-                for (int m = 1; m < R; ++m) x[m] = cmul(x[m], ld_tw(tw + (m - 1) * P + k));
+                for (int m = 1; m < R; ++m) x[m] = twiddle_mul<Eng>(x[m], ld_tw(tw + (m - 1) * P + k));
             }
             eng.template run<R>(x);
 #pragma unroll

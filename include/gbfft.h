@@ -253,6 +253,13 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
  *                                          memory and back around every transform
  *                                          instead of the transform reading and
  *                                          writing them itself
+ *   GBFFT_PREFAULT=0                       do not populate absent pages of a pageable
+ *                                          output before the GPU writes it (by
+ *                                          default outputs of 128 KB and more are
+ *                                          checked with mincore and their absent
+ *                                          pages populated: a GPU write to a page
+ *                                          the process has never touched faults
+ *                                          through the SMMU, ~20 us per 64 KB page)
  *   GBFFT_DEVICE_ALLOC_CAP=<bytes>         device requests above it fail with
  *                                          GBFFT_ERR_OUT_OF_MEMORY (tests the
  *                                          out-of-memory paths without a real one) */

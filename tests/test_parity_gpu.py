@@ -519,3 +519,30 @@ def test_host_pinned_batches(gpu_ctx, oracle, torch_cuda, logn, batch):
     torch.cuda.synchronize()
     assert np.array_equal(hx.numpy(), want.cpu().numpy())
     assert oracle.rel_l2(hx.numpy(), oracle.fft64(x)) <= TOL_REL_L2
+
+
+@pytest.mark.parametrize("prefault", ["1", "0"])
+def test_host_fresh_output_pages(monkeypatch, oracle, lib_built, prefault):
+    """A freshly allocated (never touched) pageable output, contiguous and as
+    separate rows: the library populates its absent pages before the GPU
+    writes them (GBFFT_PREFAULT=0 leaves that to the GPU's own faults); both
+    give the same bits, in place too."""
+    import gbfft
+    from gbfft import signals
+    monkeypatch.setenv("GBFFT_PREFAULT", prefault)
+    n, batch = 4096, 2048  # 64 MB: above the allocator's mmap threshold, so fresh pages
+    x = signals.normal_c64(batch, n, seed=1500)
+    with gbfft.Context(0) as ctx:
+        out = np.empty_like(x)
+        ctx.c2c_host(x, gbfft.FORWARD, out=out)
+        rows = [np.empty(1 << 17, np.complex64) for _ in range(3)]  # 1 MB rows, fresh pages
+        src = [signals.normal_c64(1, 1 << 17, seed=1501 + i)[0] for i in range(3)]
+        got = ctx.c2c_host_rows(src, gbfft.FORWARD)
+        y = x.copy()
+        ctx.c2c_host(y, gbfft.FORWARD, out=y)  # in place: the input's pages are present and kept
+    want = oracle.fft64(x[::256])
+    assert oracle.rel_l2(out[::256], want) <= 2e-6
+    assert np.array_equal(out, y)
+    for s, g in zip(src, got):
+        assert oracle.rel_l2(g[None], oracle.fft64(s[None])) <= 2e-6
+    del rows

@@ -536,7 +536,26 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
 // safe).  Separate rows are merged into runs of adjacent or overlapping pages,
 // so heap-allocated rows cost a few calls.  Failures (older kernels, special
 // mappings) are ignored: the GPU then faults the pages in itself.
-static void prefault_pages(uintptr_t lo, uintptr_t hi, uintptr_t page) {
+// Populating means the kernel zeroing every absent page (~5 ms for 128 MB on
+// one thread); runs of 8 MB and more are split over the context's copy threads.
+static void populate_run(gbfft_ctx *ctx, uintptr_t lo, uintptr_t hi, uintptr_t page) {
+    const size_t len = hi - lo;
+    if (len < ((size_t)8 << 20)) {
+        (void)madvise((void *)lo, len, MADV_POPULATE_WRITE);
+        return;
+    }
+    if (!ctx->copy_pool) {
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        ctx->copy_pool.reset(new CopyPool(std::min(kCopyThreads, hw)));
+    }
+    const size_t piece = ((len / ctx->copy_pool->size()) + page - 1) & ~(page - 1);
+    ctx->copy_pool->run([&](unsigned k, unsigned) {
+        const uintptr_t a = lo + k * piece;
+        if (a < hi) (void)madvise((void *)a, std::min<size_t>(piece, hi - a), MADV_POPULATE_WRITE);
+    });
+}
+
+static void prefault_pages(gbfft_ctx *ctx, uintptr_t lo, uintptr_t hi, uintptr_t page) {
     if (hi <= lo) return;
     const size_t npages = (hi - lo) / page;
     // Present memory, the usual case of a reused output, is recognised from
@@ -555,7 +574,7 @@ static void prefault_pages(uintptr_t lo, uintptr_t hi, uintptr_t page) {
     thread_local std::vector<unsigned char> present;
     if (present.size() < npages) present.resize(npages);
     if (mincore((void *)lo, hi - lo, present.data()) != 0) {
-        (void)madvise((void *)lo, hi - lo, MADV_POPULATE_WRITE);
+        populate_run(ctx, lo, hi, page);
         return;
     }
     for (size_t i = 0; i < npages;) {
@@ -565,7 +584,7 @@ static void prefault_pages(uintptr_t lo, uintptr_t hi, uintptr_t page) {
         }
         size_t j = i;
         while (j < npages && !(present[j] & 1)) ++j;
-        (void)madvise((void *)(lo + i * page), (j - i) * page, MADV_POPULATE_WRITE);
+        populate_run(ctx, lo + i * page, lo + j * page, page);
         i = j;
     }
 }
@@ -578,14 +597,15 @@ static void prefault_pages(uintptr_t lo, uintptr_t hi, uintptr_t page) {
 // whole batch is examined (a first call, or a heap that has just grown).
 // Outputs below 128 KB in all are not checked: a call that small would pay
 // more for the check (~2 us of a 13 us single-row call) than it can save.
-static void prefault_output(char *base, size_t bytes, float *const *rows, uint64_t nrows, size_t row_bytes) {
+static void prefault_output(gbfft_ctx *ctx, char *base, size_t bytes, float *const *rows, uint64_t nrows,
+                            size_t row_bytes) {
     constexpr size_t kMmapBytes = 128 << 10;
     static const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
     auto down = [](uintptr_t a) { return a & ~(page - 1); };
     auto up = [](uintptr_t a) { return (a + page - 1) & ~(page - 1); };
     if (bytes < kMmapBytes) return;
     if (!rows) {
-        prefault_pages(down((uintptr_t)base), up((uintptr_t)base + bytes), page);
+        prefault_pages(ctx, down((uintptr_t)base), up((uintptr_t)base + bytes), page);
         return;
     }
     if (row_bytes < kMmapBytes) {
@@ -603,12 +623,12 @@ static void prefault_output(char *base, size_t bytes, float *const *rows, uint64
             lo = std::min(lo, a);
             hi = std::max(hi, b);
         } else {
-            prefault_pages(lo, hi, page);
+            prefault_pages(ctx, lo, hi, page);
             lo = a;
             hi = b;
         }
     }
-    prefault_pages(lo, hi, page);
+    prefault_pages(ctx, lo, hi, page);
 }
 
 // Host batch in pageable memory (contiguous at in_base/out_base, or separate
@@ -643,7 +663,7 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     if (!allow_gather && !(single && !in_rows) && !pair) return kNotDirect;
     // (allow_gather is false only for pinned batches, whose pages are present)
     if (ctx->prefault && allow_gather && batch > 0)
-        prefault_output(out_base, bytes, in_rows ? out_rows : nullptr, batch, row_bytes);
+        prefault_output(ctx, out_base, bytes, in_rows ? out_rows : nullptr, batch, row_bytes);
     if (in_rows && batch == 1 && !pair) {  // one row: its own address is the base, no pointer table
         in_base = (const char *)in_rows[0];
         out_base = (char *)out_rows[0];

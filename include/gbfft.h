@@ -244,6 +244,7 @@ int gbfft_autotune(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, do
 
 /* Environment read by the library:
  *   GBFFT_AUTOTUNE, GBFFT_AUTOTUNE_CACHE   see gbfft_autotune
+ *   GBFFT_AUTOTUNE_VERBOSE=1               print every timed plan variant to stderr
  *   GBFFT_PRECISION=tc_fp16|tc_bf16x3|tc_tf32|tc_bf16x6  default precision of new contexts
  *   GBFFT_HOST_CHUNK_BYTES=<bytes>         chunk of the host-batch pipeline (32 MB)
  *   GBFFT_HOST_PATH=staged                 pageable host batches go through pinned

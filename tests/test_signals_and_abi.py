@@ -97,3 +97,18 @@ def test_product_does_not_reference_oracle():
             if f.endswith((".py", ".cu", ".cuh", ".h", ".cpp", ".hpp")):
                 text = open(os.path.join(dirpath, f)).read()
                 assert "liboracle" not in text and "import oracle" not in text, f
+
+
+def test_every_environment_variable_is_documented():
+    """Every GBFFT_* variable the library reads with getenv appears in the
+    header's environment list."""
+    csrc = os.path.join(ROOT, "wgls-rs-fft_gb300", "csrc")
+    read = set()
+    for f in os.listdir(csrc):
+        if f.endswith((".cu", ".cuh", ".h")):
+            read |= set(re.findall(r'getenv\("(GBFFT_[A-Z0-9_]+)"\)', open(os.path.join(csrc, f)).read()))
+    header = open(os.path.join(ROOT, "include", "gbfft.h")).read()
+    env_doc = header[header.index("Environment read by the library"):]
+    assert read, "no getenv found"
+    missing = sorted(v for v in read if not re.search(r"\b%s\b" % v, env_doc))
+    assert not missing, missing

@@ -180,8 +180,10 @@ __device__ __forceinline__ void rag_loop(const RagParams &P, float2 *smem_rag, E
     for (uint32_t par = 0;; par ^= 1u) {
         const uint32_t idx = s_item[par];
         if (idx >= P.nitems) break;
-        // (slot par ^ 1 was last read before the previous item's final barrier)
-        if (threadIdx.x == 0) s_item[par ^ 1u] = rag_claim(P);
+        // The next claim's result stays in a register until the item's end:
+        // storing it at once would hold warp 0 for the atomic's round trip.
+        uint32_t next = 0;
+        if (threadIdx.x == 0) next = rag_claim(P);
         const RagItem it = P.items[idx];
         bool ok = true;
         if (it.kind == 0) {
@@ -200,6 +202,8 @@ __device__ __forceinline__ void rag_loop(const RagParams &P, float2 *smem_rag, E
             ok = rag_pass_dispatch<false>(P, it, smem_rag, eng);
         }
         if (!ok) break;
+        // (slot par ^ 1 was last read before the previous item's final barrier)
+        if (threadIdx.x == 0) s_item[par ^ 1u] = next;
         __syncthreads();  // the item's stores are issued; shared memory is free
         if (it.kind == 1 && threadIdx.x == 0) {
             // publish: the barrier ordered the CTA's stores before this fence

@@ -697,9 +697,6 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
             align_bits |= a | b;
         }
         GB_CUDA(ctx, cudaMemcpyAsync(ctx->dtable.ptr, ctx->htable, tbytes, cudaMemcpyHostToDevice, ctx->xfer[0]));
-        GB_CUDA(ctx, cudaEventRecord(ctx->ev_table, ctx->xfer[0]));
-        GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[1], ctx->ev_table, 0));
-        GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[2], ctx->ev_table, 0));
         tin = (const uint64_t *)ctx->dtable.ptr;
         tout = tin + batch;
     } else {
@@ -758,6 +755,11 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
         if (plan->passes.size() >= 3) rows_per_chunk = batch;
     }
     const size_t nchunks = (batch + rows_per_chunk - 1) / rows_per_chunk;
+    if (tin) {  // the other two streams read the table that xfer[0] uploads
+        GB_CUDA(ctx, cudaEventRecord(ctx->ev_table, ctx->xfer[0]));
+        GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[1], ctx->ev_table, 0));
+        GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[2], ctx->ev_table, 0));
+    }
     size_t c = 0;
     for (uint64_t r0 = 0; r0 < batch; r0 += rows_per_chunk, ++c) {
         const uint64_t rows = std::min(batch - r0, rows_per_chunk);

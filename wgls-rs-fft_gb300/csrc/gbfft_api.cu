@@ -645,6 +645,9 @@ static void prefault_output(gbfft_ctx *ctx, char *base, size_t bytes, float *con
 // kNotDirect: returned (before any work) when allow_gather is false and the
 // shape would need the gather / scatter route, so the caller takes its own.
 constexpr int kNotDirect = -1;
+// Row batches up to this size pass their row-address table to the kernels in
+// pinned host memory instead of uploading it.
+constexpr uint64_t kHostTableRows = 64;
 static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int direction, const char *in_base,
                                 char *out_base, const float *const *in_rows, float *const *out_rows,
                                 bool allow_gather = true) {
@@ -687,8 +690,15 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
             }
             ctx->htable_bytes = tbytes;
         }
-        st = ctx->dtable.ensure(tbytes, ctx->err);
-        if (st != GBFFT_OK) return st;
+        // A small batch's kernels read the table straight from its pinned
+        // host copy (this path runs only where the GPU reaches host memory):
+        // no upload to wait for.  Larger batches upload it once, since every
+        // CTA would otherwise start with a read across the host link.
+        const bool host_table = batch <= kHostTableRows;
+        if (!host_table) {
+            st = ctx->dtable.ensure(tbytes, ctx->err);
+            if (st != GBFFT_OK) return st;
+        }
         for (uint64_t r = 0; r < batch; ++r) {
             const uintptr_t a = in_rows ? (uintptr_t)in_rows[r] : (uintptr_t)(in_base + r * row_bytes);
             const uintptr_t b = in_rows ? (uintptr_t)out_rows[r] : (uintptr_t)(out_base + r * row_bytes);
@@ -696,8 +706,13 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
             ctx->htable[batch + r] = (uint64_t)b;
             align_bits |= a | b;
         }
-        GB_CUDA(ctx, cudaMemcpyAsync(ctx->dtable.ptr, ctx->htable, tbytes, cudaMemcpyHostToDevice, ctx->xfer[0]));
-        tin = (const uint64_t *)ctx->dtable.ptr;
+        if (host_table) {
+            tin = ctx->htable;
+        } else {
+            GB_CUDA(ctx,
+                    cudaMemcpyAsync(ctx->dtable.ptr, ctx->htable, tbytes, cudaMemcpyHostToDevice, ctx->xfer[0]));
+            tin = (const uint64_t *)ctx->dtable.ptr;
+        }
         tout = tin + batch;
     } else {
         align_bits = (uintptr_t)in_base | (uintptr_t)out_base;
@@ -755,7 +770,7 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
         if (plan->passes.size() >= 3) rows_per_chunk = batch;
     }
     const size_t nchunks = (batch + rows_per_chunk - 1) / rows_per_chunk;
-    if (tin) {  // the other two streams read the table that xfer[0] uploads
+    if (tin && tin != ctx->htable) {  // the other two streams read the table that xfer[0] uploads
         GB_CUDA(ctx, cudaEventRecord(ctx->ev_table, ctx->xfer[0]));
         GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[1], ctx->ev_table, 0));
         GB_CUDA(ctx, cudaStreamWaitEvent(ctx->xfer[2], ctx->ev_table, 0));

@@ -27,8 +27,8 @@ struct RowsCfg : SubCfg<LOGN, LE> {
 // DIRC: -1 forward, +1 inverse (a launch has one direction, so the sign and
 // scale work is resolved at compile time).
 // TAB: rows addressed through tables instead of in / out: row r is read from
-// tab_in[r] and written to tab_out[r] (device arrays of the rows' own
-// addresses).  The host entries pass the caller's separate host rows this
+// tab_in[r] and written to tab_out[r] (arrays of the rows' own addresses, in
+// device memory or, for small batches, pinned host memory).  The host entries pass the caller's separate host rows this
 // way; the GPU reads and writes them through the host's page tables, so a
 // host batch needs no copy in HBM.  A separate instantiation, so the
 // contiguous kernels are unchanged.

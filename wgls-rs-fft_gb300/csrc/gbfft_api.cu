@@ -676,7 +676,7 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     }
     const uint64_t *tin = nullptr, *tout = nullptr;
     uintptr_t align_bits = 0;
-    if (in_rows || pair) {  // row addresses as device tables (the fused pair reads rows through them only)
+    if (in_rows || pair) {  // row addresses as tables the kernels read (the fused pair reads rows through them only)
         const size_t tbytes = 2 * batch * sizeof(uint64_t);
         if (ctx->htable_bytes < tbytes) {
             if (ctx->htable) cudaFreeHost(ctx->htable);

@@ -55,8 +55,9 @@ cudaError_t rows_prepare(RowsKernelInfo &k);
 // Sets fn_tab / fn_tab_inv for the tile (null where no table form is built).
 void rows_tab_describe(int logn, int logs, int loge, RowsKernelInfo &k);
 // persistent: use fn_persistent with at most persist_ctas_per_sm * sms CTAs.
-// tab_in / tab_out: device arrays of per-row addresses (row r read from
-// tab_in[r], written to tab_out[r]; in / out ignored); never persistent.
+// tab_in / tab_out: arrays of per-row addresses the device can read (row r
+// read from tab_in[r], written to tab_out[r]; in / out ignored); never
+// persistent.
 cudaError_t rows_launch(const RowsKernelInfo &k, const float2 *in, float2 *out, uint64_t batch,
                         const float2 *tw, int direction, int logn, bool persistent, int sms, cudaStream_t stream,
                         LoadOps ops = LoadOps{nullptr, 0u, 0.f, 0u}, const uint64_t *tab_in = nullptr,

@@ -7,9 +7,6 @@
 //   SizeCache / build_size_cache -> Plan / plan_for     (src/lib.rs:230-259, 709-943)
 //   benchmark_gpu_only           -> gbfft_bench_device  (src/lib.rs:673-707)
 // plus the device-resident entry gbfft_c2c_device.
-#include <sys/mman.h>
-#include <unistd.h>
-
 #include <cstdarg>
 #include <cstdio>
 #include <cstdlib>
@@ -28,6 +25,7 @@
 #include "gbfft_internal.h"
 #include "gbfft_plan.h"
 #include "gbfft_ragged.h"
+#include "host_pages.h"
 
 using namespace gbfft;
 
@@ -521,116 +519,25 @@ static int host_pipeline(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int directi
     return check_device_flag(ctx);
 }
 
-#ifndef MADV_POPULATE_WRITE
-#define MADV_POPULATE_WRITE 23  // Linux 5.14
-#endif
-
-// Pageable output memory that the GPU is about to write through the host's
-// page tables: make its pages present first.  A GPU write to a page the
-// process has not touched yet (a fresh allocation) faults through the SMMU, at
-// about 20 us per 64 KB page on Grace: a freshly allocated 128 MB output took
-// 37 ms against 1.2 ms once present (5.2 ms populated first).  mincore()
-// finds the absent pages (populating every page of present memory cost 3 ms
-// per 512 MB call), and madvise(MADV_POPULATE_WRITE) populates each run of
-// them in one call without changing their contents (in-place calls are
-// safe).  Separate rows are merged into runs of adjacent or overlapping pages,
-// so heap-allocated rows cost a few calls.  Failures (older kernels, special
-// mappings) are ignored: the GPU then faults the pages in itself.
-//
-// populate_run: populating means the kernel zeroing every absent page (~5 ms
-// for 128 MB on one thread); runs of 8 MB and more are split over the
-// context's copy threads (6.3 -> 5.2 ms for 128 MB).
-static void populate_run(gbfft_ctx *ctx, uintptr_t lo, uintptr_t hi, uintptr_t page) {
+// Populating means the kernel zeroing every absent page (~5 ms for 128 MB on
+// one thread); runs of 8 MB and more are split over the context's copy
+// threads (6.3 -> 5.2 ms for 128 MB).  See host_pages.h for when and why.
+static void populate_run(gbfft_ctx *ctx, uintptr_t lo, uintptr_t hi) {
     const size_t len = hi - lo;
     if (len < ((size_t)8 << 20)) {
-        (void)madvise((void *)lo, len, MADV_POPULATE_WRITE);
+        populate_pages(lo, hi);
         return;
     }
     if (!ctx->copy_pool) {
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         ctx->copy_pool.reset(new CopyPool(std::min(kCopyThreads, hw)));
     }
+    const uintptr_t page = host_page_size();
     const size_t piece = ((len / ctx->copy_pool->size()) + page - 1) & ~(page - 1);
     ctx->copy_pool->run([&](unsigned k, unsigned) {
         const uintptr_t a = lo + k * piece;
-        if (a < hi) (void)madvise((void *)a, std::min<size_t>(piece, hi - a), MADV_POPULATE_WRITE);
+        if (a < hi) populate_pages(a, a + std::min<size_t>(piece, hi - a));
     });
-}
-
-static void prefault_pages(gbfft_ctx *ctx, uintptr_t lo, uintptr_t hi, uintptr_t page) {
-    if (hi <= lo) return;
-    const size_t npages = (hi - lo) / page;
-    // Present memory, the usual case of a reused output, is recognised from
-    // four sampled pages (each mincore call costs ~3 us here; a whole-range
-    // check of a 512 MB output cost 1.4 % of the call); a range whose samples
-    // are all present is left to the GPU.
-    if (npages > 4) {
-        bool all = true;
-        for (size_t k = 0; k < 4 && all; ++k) {
-            unsigned char v = 0;
-            const uintptr_t pg = lo + (k * (npages - 1) / 3) * page;
-            all = mincore((void *)pg, page, &v) == 0 && (v & 1);
-        }
-        if (all) return;
-    }
-    thread_local std::vector<unsigned char> present;
-    if (present.size() < npages) present.resize(npages);
-    if (mincore((void *)lo, hi - lo, present.data()) != 0) {
-        populate_run(ctx, lo, hi, page);
-        return;
-    }
-    for (size_t i = 0; i < npages;) {
-        if (present[i] & 1) {
-            ++i;
-            continue;
-        }
-        size_t j = i;
-        while (j < npages && !(present[j] & 1)) ++j;
-        populate_run(ctx, lo + i * page, lo + j * page, page);
-        i = j;
-    }
-}
-
-// Which outputs are checked: a contiguous output (or a single row) of at least
-// 128 KB, and separate rows of at least 128 KB each -- the sizes the C library
-// allocates with a fresh mmap, so a per-call output vector is absent every
-// call.  Smaller rows come from the heap, recycled and present in steady
-// state; for them three sampled rows (first, middle, last) decide whether the
-// whole batch is examined (a first call, or a heap that has just grown).
-// Outputs below 128 KB in all are not checked: a call that small would pay
-// more for the check (~2 us of a 13 us single-row call) than it can save.
-static void prefault_output(gbfft_ctx *ctx, char *base, size_t bytes, float *const *rows, uint64_t nrows,
-                            size_t row_bytes) {
-    constexpr size_t kMmapBytes = 128 << 10;
-    static const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
-    auto down = [](uintptr_t a) { return a & ~(page - 1); };
-    auto up = [](uintptr_t a) { return (a + page - 1) & ~(page - 1); };
-    if (bytes < kMmapBytes) return;
-    if (!rows) {
-        prefault_pages(ctx, down((uintptr_t)base), up((uintptr_t)base + bytes), page);
-        return;
-    }
-    if (row_bytes < kMmapBytes) {
-        bool present = true;
-        for (uint64_t r : {(uint64_t)0, nrows / 2, nrows - 1}) {
-            unsigned char v = 0;
-            present = present && mincore((void *)down((uintptr_t)rows[r]), page, &v) == 0 && (v & 1);
-        }
-        if (present) return;
-    }
-    uintptr_t lo = 0, hi = 0;
-    for (uint64_t r = 0; r < nrows; ++r) {
-        const uintptr_t a = down((uintptr_t)rows[r]), b = up((uintptr_t)rows[r] + row_bytes);
-        if (hi > lo && a <= hi && b >= lo) {
-            lo = std::min(lo, a);
-            hi = std::max(hi, b);
-        } else {
-            prefault_pages(ctx, lo, hi, page);
-            lo = a;
-            hi = b;
-        }
-    }
-    prefault_pages(ctx, lo, hi, page);
 }
 
 // Host batch in pageable memory (contiguous at in_base/out_base, or separate
@@ -668,7 +575,8 @@ static int host_pipeline_direct(gbfft_ctx *ctx, uint64_t n, uint64_t batch, int 
     if (!allow_gather && !(single && !in_rows) && !pair) return kNotDirect;
     // (allow_gather is false only for pinned batches, whose pages are present)
     if (ctx->prefault && allow_gather && batch > 0)
-        prefault_output(ctx, out_base, bytes, in_rows ? out_rows : nullptr, batch, row_bytes);
+        prefault_output(out_base, bytes, in_rows ? out_rows : nullptr, batch, row_bytes,
+                        [ctx](uintptr_t lo, uintptr_t hi) { populate_run(ctx, lo, hi); });
     if (in_rows && batch == 1 && !pair) {  // one row: its own address is the base, no pointer table
         in_base = (const char *)in_rows[0];
         out_base = (char *)out_rows[0];

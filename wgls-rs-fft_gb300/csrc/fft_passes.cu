@@ -153,9 +153,9 @@ fft_pass_first_tma_kernel(const __grid_constant__ CUtensorMap map, float2 *out, 
                           uint32_t *err) {
     using T = PassTmaCfg<LOGR, LE>;
     constexpr int R = 1 << LOGR;
-    extern __shared__ __align__(1024) float2 smem_pass[];
-    uint64_t *bar = (uint64_t *)((char *)smem_pass + T::OFF_BAR);
-    int *s_fail = (int *)((char *)smem_pass + T::OFF_BAR + 8);
+    extern __shared__ __align__(1024) float2 smem_tma[];
+    uint64_t *bar = (uint64_t *)((char *)smem_tma + T::OFF_BAR);
+    int *s_fail = (int *)((char *)smem_tma + T::OFF_BAR + 8);
     const int lognc = logn - LOGR;
     const uint64_t tile = blockIdx.x;
     const uint64_t b = tile >> (lognc - 3);
@@ -171,7 +171,7 @@ fft_pass_first_tma_kernel(const __grid_constant__ CUtensorMap map, float2 *out, 
                      : "memory");
 #pragma unroll
         for (int k = 0; k < R / kTmaBoxRows; ++k)
-            tma_load_3d(smem_u32(smem_pass + k * kTmaBoxRows * 8), &map, (int)(2 * col0), k * kTmaBoxRows, (int)b,
+            tma_load_3d(smem_u32(smem_tma + k * kTmaBoxRows * 8), &map, (int)(2 * col0), k * kTmaBoxRows, (int)b,
                         smem_u32(bar));
     }
     uint32_t polls = 0;
@@ -204,7 +204,7 @@ fft_pass_first_tma_kernel(const __grid_constant__ CUtensorMap map, float2 *out, 
     a.coherent_load = false;
     a.row = (uint32_t)b;
     a.ops = ops;
-    pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_pass);
+    pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_tma);
 }
 
 __device__ __forceinline__ void tma_prefetch_3d(const CUtensorMap *map, int x, int y, int z) {
@@ -226,9 +226,9 @@ fft_pass_first_tma_persistent_kernel(const __grid_constant__ CUtensorMap map, fl
                                      uint32_t *err, uint64_t ntiles) {
     using T = PassTmaCfg<LOGR, LE>;
     constexpr int R = 1 << LOGR;
-    extern __shared__ __align__(1024) float2 smem_pass[];
-    uint64_t *bar = (uint64_t *)((char *)smem_pass + T::OFF_BAR);
-    int *s_fail = (int *)((char *)smem_pass + T::OFF_BAR + 8);
+    extern __shared__ __align__(1024) float2 smem_tma[];
+    uint64_t *bar = (uint64_t *)((char *)smem_tma + T::OFF_BAR);
+    int *s_fail = (int *)((char *)smem_tma + T::OFF_BAR + 8);
     const int lognc = logn - LOGR;
     const uint64_t per_row = 1ull << (lognc - 3);  // tiles a transform
     if (threadIdx.x == 0) {
@@ -249,7 +249,7 @@ fft_pass_first_tma_persistent_kernel(const __grid_constant__ CUtensorMap map, fl
                          : "memory");
 #pragma unroll
             for (int k = 0; k < R / kTmaBoxRows; ++k)
-                tma_load_3d(smem_u32(smem_pass + k * kTmaBoxRows * 8), &map, (int)(2 * col0), k * kTmaBoxRows,
+                tma_load_3d(smem_u32(smem_tma + k * kTmaBoxRows * 8), &map, (int)(2 * col0), k * kTmaBoxRows,
                             (int)b, smem_u32(bar));
             const uint64_t next = tile + gridDim.x;
             if (next < ntiles) {
@@ -289,7 +289,7 @@ fft_pass_first_tma_persistent_kernel(const __grid_constant__ CUtensorMap map, fl
         a.coherent_load = false;
         a.row = (uint32_t)b;
         a.ops = ops;
-        pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_pass);
+        pass_tile<LOGR, 1, true, DftRegs, 0, -1, LE, 3, true>(a, smem_tma);
         __syncthreads();  // every read of the shared tile is done before the next tile's copies
     }
 }

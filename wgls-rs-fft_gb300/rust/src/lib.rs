@@ -121,6 +121,33 @@ impl GpuFft {
         Ok(out)
     }
 
+    /// `fft` (or, with `inverse`, `ifft`) into caller-provided rows of the
+    /// inputs' lengths; `outputs[i]` may be `inputs[i]`'s length-matched
+    /// buffer from an earlier call.  Reused output rows stay resident, so the
+    /// GPU writes them at the host link's rate; a freshly allocated row of
+    /// 128 KB or more has its absent pages populated by the library first.
+    pub fn transform_into(
+        &self,
+        inputs: &[Vec<Complex<f32>>],
+        outputs: &mut [Vec<Complex<f32>>],
+        inverse: bool,
+    ) -> Result<(), Box<dyn Error>> {
+        if outputs.len() != inputs.len() || inputs.iter().zip(outputs.iter()).any(|(a, b)| a.len() != b.len()) {
+            return Err(status_msg(GBFFT_ERR_INVALID_ARGUMENT).into());
+        }
+        if inputs.is_empty() {
+            return Ok(());
+        }
+        let dir = if inverse { GBFFT_INVERSE } else { GBFFT_FORWARD };
+        let ins: Vec<*const f32> = inputs.iter().map(|r| r.as_ptr() as *const f32).collect();
+        let lens: Vec<u64> = inputs.iter().map(|r| r.len() as u64).collect();
+        let outs: Vec<*mut f32> = outputs.iter_mut().map(|r| r.as_mut_ptr() as *mut f32).collect();
+        let st = unsafe {
+            gbfft_c2c_host_rows(self.ctx, ins.as_ptr(), lens.as_ptr(), outs.as_ptr(), inputs.len() as u64, dir)
+        };
+        self.check(st)
+    }
+
     /// A contiguous batch (`batch` rows of `n` samples, row-major) in one call.
     pub fn fft_contiguous(
         &self,

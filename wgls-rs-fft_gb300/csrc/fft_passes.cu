@@ -413,7 +413,7 @@ cudaError_t pass_launch(const PassDesc &d, const float2 *in, float2 *out, uint64
     if (d.cols < kCols && ((uintptr_t)out & 15u)) return cudaErrorMisalignedAddress;
     int logp = d.logp;
     // tensor-map first pass: needs a 16-byte aligned input (the map's base
-    // address), an error flag for its bounded wait, and the driver's encoder;
+    // address), an error flag for its bounded wait, and the CUDA driver's encoder;
     // otherwise the LDG kernel runs
     PFN_cuTensorMapEncodeTiled_v12000 encode = d.fn_tma ? tensor_map_encoder() : nullptr;
     if (d.fn_tma && encode && err && ((uintptr_t)in & 15u) == 0 && tiles <= 0x7fffffffull && batch <= 0xffffffffull) {

@@ -14,7 +14,7 @@
 // Where its memory comes from: two file-scope device arrays of this library,
 // a 32 MiB scratch buffer for the intermediate result between the two global
 // passes, and a 256 KiB table area for the twiddles of every supported size.
-// The driver reserves them when it loads this library's code on a GPU; every
+// The CUDA driver reserves them when it loads this library's code on a GPU; every
 // GPU that loads the library holds them until the process exits.
 //
 // Speed: it runs one launch per global pass with 16 samples a thread, the

@@ -69,6 +69,26 @@ class GpuFft : public FftExecutor {
     // GpuFft::ifft (src/lib.rs:483-488): inverse scaled by 1/N.
     Batch ifft(const Batch &inputs) override { return run(inputs, GBFFT_INVERSE); }
 
+    // fft / ifft into caller-kept output rows of the inputs' lengths (no
+    // reference counterpart): reused rows stay resident, so the GPU writes
+    // them at the host link's rate.
+    void transform_into(const Batch &inputs, Batch &outputs, bool inverse = false) {
+        bool same = outputs.size() == inputs.size();
+        for (size_t i = 0; same && i < inputs.size(); ++i) same = outputs[i].size() == inputs[i].size();
+        if (!same) throw Error(GBFFT_ERR_INVALID_ARGUMENT, "output rows must have the input rows' lengths");
+        if (inputs.empty()) return;
+        const size_t b = inputs.size();
+        std::vector<const float *> in(b);
+        std::vector<uint64_t> len(b);
+        std::vector<float *> outp(b);
+        for (size_t i = 0; i < b; ++i) {
+            in[i] = reinterpret_cast<const float *>(inputs[i].data());
+            len[i] = inputs[i].size();
+            outp[i] = reinterpret_cast<float *>(outputs[i].data());
+        }
+        check(gbfft_c2c_host_rows(ctx_, in.data(), len.data(), outp.data(), b, inverse ? GBFFT_INVERSE : GBFFT_FORWARD));
+    }
+
     // Device-resident transform (no reference counterpart): interleaved
     // complex<float> device buffers, enqueued on `stream` (a cudaStream_t).
     void fft_device(const void *d_in, void *d_out, uint64_t n, uint64_t batch, int direction,

@@ -100,6 +100,13 @@ int main() {
     auto bo = fft.fft(sig);
     CHECK(bo.size() == 4, "batch count");
     for (int i = 0; i < 4; ++i) CHECK(max_diff(fft.fft({sig[i]})[0], bo[i]) < 1e-4f, "batch independence %d", i);
+    // into caller-kept rows: the same bits as fft / ifft
+    Batch kept(4, std::vector<Complex>(128));
+    fft.transform_into(sig, kept);
+    for (int i = 0; i < 4; ++i) CHECK(max_diff(kept[i], bo[i]) == 0.f, "transform_into row %d", i);
+    fft.transform_into(bo, kept, true);
+    auto bi = fft.ifft(bo);
+    for (int i = 0; i < 4; ++i) CHECK(max_diff(kept[i], bi[i]) == 0.f, "transform_into inverse row %d", i);
 
     // empty batch, errors with the reference's messages
     CHECK(fft.fft({}).empty(), "empty batch");
